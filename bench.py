@@ -1,0 +1,319 @@
+#!/usr/bin/env python
+"""JK-build throughput benchmark (one JSON line on rank 0).
+
+Workload: one RI JK build = computeJKj (J_i, K_i for all i < nbf5) at
+nbf=600, naux=2400, nbf5=300 (seeded synthetic inputs; b is 6.9 GB, larger
+than L2, so no flush is needed between steps).
+
+Legs of the default run (``--impl ours``):
+  value   builds/s with b, C resident in HBM (device-timed, CUDA events);
+  e2e     builds/s through the reference-facing drop-in call
+          ``pynof_gb300.integrals.JKj_RI_GPU(C, b, p)``: host C in (pinned),
+          host J, K out (pinned), copies inside the timed region;
+  roofline  the dominant kernel's algorithmic rate over the launch time the
+          library's event profiler recorded inside the timed region;
+  cpu_baseline  the CPU oracle (numpy/OpenBLAS, all host threads) on a
+          bounded sample of orbitals, scaled to builds/s.
+
+``--impl reference`` times the CPU restatement of PyNOF's JKj_RI (the
+reference itself is Python and is not present at run time) on the same
+workload; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "c3"
+METRIC = "RI-JK builds/s at nbf=600 (computeJKj, J_i and K_i for i < nbf5)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="orbitals in the CPU sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def flops_jkj(N, P, Q):
+    """Algorithmic flops of one RI JK build in the reference's formulation:
+    2PN^2Q (half transform) + 2PNQ (diagonal) + 2PN^2Q (J) + 2PN^2Q (K)."""
+    return 6.0 * P * N * N * Q + 2.0 * P * N * Q
+
+
+KERNEL_FLOPS = {
+    # per launch, reference formulation (symmetry the kernels exploit is not discounted)
+    "gemm_f64:half_transform": lambda N, P, Q: 2.0 * P * N * N * Q,
+    "gemm_f64:J": lambda N, P, Q: 2.0 * P * N * N * Q,
+    "gemm_f64:K": lambda N, P, Q: 2.0 * P * N * N * Q,
+    "contract_diag": lambda N, P, Q: 2.0 * P * N * Q,
+}
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, "--query-gpu=" + ",".join(self.FIELDS), "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(b, C, P, sample, N, Q):
+    """Oracle JKj_RI on the first `sample` orbitals, scaled to builds/s."""
+    from oracle import pynof_oracle as orc
+
+    cores = os.cpu_count()
+    orc.jkj_ri(C, b, 2)  # warm the BLAS threads
+    times = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        orc.jkj_ri(C, b, sample)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": (sample / P) / t, "unit": "builds/s", "cores": cores, "kind": "port",
+            "sample": f"J_i, K_i for {sample} of {P} orbitals at nbf={N}, naux={Q} (median of 5; scaled by "
+                      f"{sample}/{P}; numpy/OpenBLAS restatement of JKj_RI)",
+            "seconds_per_sample": t}
+
+
+def make_workload(name):
+    from pynof_gb300 import synthetic
+
+    st = synthetic.structure(name)
+    b, C, H, n = synthetic.make_inputs(st, 0)
+    return st, b, C, H, n
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    st, b, C, H, n = make_workload(args.workload)
+    N, P, Q = st.nbf, st.nbf5, st.nbfaux
+    from oracle import pynof_oracle as orc
+
+    sample = args.cpu_sample or max(2, P // 5)
+    orc.jkj_ri(C, b, 2)
+    for _ in range(args.warmup):
+        orc.jkj_ri(C, b, sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.jkj_ri(C, b, sample)
+    dt = time.perf_counter() - t0
+    value = args.steps * (sample / P) / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P}", "sample_orbitals": sample},
+        "cpu_baseline": {"value": value, "unit": "builds/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"J_i, K_i for {sample} of {P} orbitals per step, scaled by {sample}/{P}"},
+        "e2e": {"value": value, "unit": "builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from pynof_gb300 import _lib, integrals, ops
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    st, b, C, H, n = make_workload(args.workload)
+    N, P, Q = st.nbf, st.nbf5, st.nbfaux
+    db = ops.to_device(b)
+    dC = ops.to_device(C)
+    asym = ops.check_symmetric(db)
+    assert asym == 0.0, asym
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident leg --------------------------------------------
+    for _ in range(args.warmup):
+        J, K = ops.jkj_ri(dC, db, P)
+    del J, K
+    props = torch.cuda.get_device_properties(dev)
+    gpu_id = str(getattr(props, "uuid", local))
+    if gpu_id and not gpu_id.startswith("GPU-") and len(gpu_id) == 36:
+        gpu_id = "GPU-" + gpu_id
+    clocks = ClockSampler(gpu_id)
+    barrier()
+    clocks.start()
+    _lib.profile_start()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        J, K = ops.jkj_ri(dC, db, P)
+    e1.record(stream)
+    barrier()
+    prof = _lib.profile_stop()
+    clk = clocks.stop()
+    dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3)
+    value = world * args.steps / dev_s
+
+    # ---- end-to-end leg through the drop-in call -------------------------
+    C_pin = torch.from_numpy(C).pin_memory().numpy()
+    p = st
+    for _ in range(max(1, args.warmup)):
+        Jh, Kh = integrals.JKj_RI_GPU(C_pin, db, p)
+    del Jh, Kh
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Jh, Kh = integrals.JKj_RI_GPU(C_pin, db, p)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * args.steps / e2e_s
+    h2d = C.nbytes
+    d2h = 2 * P * N * N * 8
+
+    # ---- roofline of the dominant kernel ---------------------------------
+    peaks, peak_src = measured_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    name, (launches, total_ms) = top
+    per_launch_s = total_ms / 1e3 / launches
+    fl = KERNEL_FLOPS.get(name, lambda N, P, Q: float("nan"))(N, P, Q)
+    achieved = fl / per_launch_s / 1e12
+    fp64_peak = measure_dgemm_tflops(torch, dev)
+    roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak, "traffic": None,
+            "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 path; MEASURED_PEAKS has no FP64 figure)",
+            "flops_per_launch": fl, "ms_per_launch": 1e3 * per_launch_s,
+            "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 3)} for k, v in prof.items()}}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P} (computeJKj)", "precision": "fp64",
+                   "l2": "inputs larger than L2 (b = %.1f GB)" % (b.nbytes / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "builds/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roof,
+        "gpu_launches": sum(v[0] for v in prof.values()),
+        "clocks": clk,
+        "achieved_tflops_algorithmic": flops_jkj(N, P, Q) / (dev_s / args.steps) / 1e12,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = args.cpu_sample or max(2, P // 5)
+        line["cpu_baseline"] = cpu_baseline(b, C, P, sample, N, Q)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def measure_dgemm_tflops(torch, dev, n=8192, reps=3):
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    bm = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, bm)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, bm)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

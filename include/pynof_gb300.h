@@ -1,0 +1,111 @@
+/*
+ * libpynof_gb300 -- C ABI of the GB300 (sm_103a) RI / full-ERI JK and
+ * MO-integral path of PyNOF.
+ *
+ * Conventions shared by every entry point
+ * ---------------------------------------
+ * - Every pointer is a DEVICE pointer unless stated otherwise; every array is
+ *   row-major (numpy C order) float64, laid out exactly like the reference's
+ *   numpy arrays:
+ *       C      [nbf][nbf]            column p = MO p
+ *       H      [nbf][nbf]
+ *       b      [nbf][nbf][naux]      b[m][n][Q], symmetric in (m, n)
+ *       I      [nbf][nbf][nbf][nbf]  I[m][n][s][l] = (mn|sl), 8-fold symmetric
+ *       J, K   [nbf5][nbf][nbf]
+ *       n      [nbf5];  cj12, ck12 [nbf5][nbf5]
+ * - nbf5 <= nbf.  Sizes are in elements.
+ * - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *   asynchronous with respect to the host; results are valid once the stream
+ *   has been synchronised.
+ * - Scratch memory comes from the caller: `workspace` must hold at least the
+ *   number of bytes the matching *_workspace_* query returns.  The library
+ *   allocates no device memory and never frees caller memory.
+ * - The return value is a GB_* status; gb_last_error() returns the message of
+ *   the last failing call on the calling thread.
+ * - The RI entry points use the (m, n) symmetry of b: J is computed on the
+ *   pairs n >= m and mirrored.  PyNOF's b_mnl is symmetric by construction
+ *   (pynof/integrals.py:39-49 builds it from the (P|mn) integrals);
+ *   gb_check_symmetric_f64 verifies a buffer.
+ */
+#ifndef PYNOF_GB300_H
+#define PYNOF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_OK 0
+#define GB_ERR_INVALID_ARG 1
+#define GB_ERR_BAD_SHAPE 2
+#define GB_ERR_WORKSPACE 3
+#define GB_ERR_CUDA 4
+#define GB_ERR_TIMEOUT 5
+#define GB_ERR_NONFINITE 6
+#define GB_ERR_UNSUPPORTED 7
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* gb_last_error(void);
+/* Library version, major * 10000 + minor * 100 + patch. */
+int gb_version(void);
+
+/* Launch profiler.  While enabled, every kernel the library launches is
+ * bracketed by two CUDA events on its stream.  gb_profile_stop synchronises on
+ * those events and writes a JSON object {"kernel": [launches, total_ms], ...}
+ * into out (host buffer of out_len bytes). */
+int gb_profile_start(void);
+int gb_profile_stop(char* out, size_t out_len);
+
+/* Maximum |b[m][n][l] - b[n][m][l]| over the tensor, written to *max_abs_diff
+ * (a DEVICE pointer to one double). */
+int gb_check_symmetric_f64(const double* b, int nbf, int naux, double* max_abs_diff, void* stream);
+
+/* ------------------------------------------------------------------------
+ * A1  computeJKj, RI.  Replaces JKj_RI_GPU (pynof/integrals.py:234-245),
+ *     dispatched from computeJKj (pynof/integrals.py:172-191).
+ *     J[q][m][n] = sum_l (sum_n' C[n'][q] (sum_m' C[m'][q] b[m'][n'][l])) b[m][n][l]
+ *     K[q][m][n] = sum_l T[q][m][l] T[q][n][l],  T[q][n][l] = sum_m' C[m'][q] b[m'][n][l]
+ *     for q < nbf5.
+ * ---------------------------------------------------------------------- */
+size_t gb_jkj_ri_workspace_f64(int nbf, int nbf5, int naux);
+int gb_jkj_ri_f64(const double* C, const double* b, int nbf, int nbf5, int naux, double* J, double* K,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * A3  computeJKH_MO, RI.  Replaces JKH_MO_RI_GPU (pynof/integrals.py:383-399),
+ *     dispatched from computeJKH_MO (pynof/integrals.py:307-326).
+ *     J_MO[p][q] = (pp|qq), K_MO[p][q] = (pq|pq), H_core[p] = C_p^T H C_p.
+ * ---------------------------------------------------------------------- */
+size_t gb_jkh_mo_ri_workspace_f64(int nbf, int nbf5, int naux);
+int gb_jkh_mo_ri_f64(const double* C, const double* H, const double* b, int nbf, int nbf5, int naux,
+                     double* J_MO, double* K_MO, double* H_core, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
+/* ------------------------------------------------------------------------
+ * A5  Integrals_MO_RI.  Replaces Integrals_MO_RI_GPU (pynof/integrals.py:709-714),
+ *     dispatched from JKH_MO_tmp (pynof/integrals.py:665-682).
+ *     Hmat[i][j] = (C^T H C)[i][j] (j < nbf5),  bMO[a][q][l] = sum_mn C[m][a] C[n][q] b[m][n][l].
+ *     Hmat is [nbf][nbf5], bMO is [nbf][nbf5][naux].
+ * ---------------------------------------------------------------------- */
+size_t gb_mo_ri_workspace_f64(int nbf, int nbf5, int naux);
+int gb_mo_ri_f64(const double* C, const double* H, const double* b, int nbf, int nbf5, int naux, double* Hmat,
+                 double* bMO, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * A5  computeLagrange2, RI, closed shell (MSpin == 0).  Replaces the GPU
+ *     branch of computeLagrange2 (pynof/utils.py:262-327).  elag is [nbf][nbf]
+ *     (columns >= nbf5 are zero), Hmat [nbf][nbf5].  The diagonals of cj12 and
+ *     ck12 are ignored (the reference zeroes them, utils.py:269-270).
+ * ---------------------------------------------------------------------- */
+size_t gb_lagrange2_ri_workspace_f64(int nbf, int nbf5, int naux);
+int gb_lagrange2_ri_f64(const double* C, const double* H, const double* b, const double* n,
+                        const double* cj12, const double* ck12, int nbf, int nbf5, int naux, int nbeta,
+                        int nalpha, double* elag, double* Hmat, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYNOF_GB300_H */

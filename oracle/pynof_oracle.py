@@ -1,0 +1,267 @@
+"""CPU oracle for the RI / full-ERI JK and MO-integral path of PyNOF.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: the parity tests, the
+smoke check and the CPU-baseline leg of the benchmark import it.  Nothing in
+the ``pynof_gb300`` package imports it, and no product code path runs through
+it.
+
+It restates, in plain numpy FP64, the algorithms of PyNOF 1.4 (``src/pynof``)
+for the functions the CUDA path replaces.  Each function names the reference
+lines it follows.  Parity of this restatement is pinned against golden vectors
+produced by the reference's own functions (``tests/golden/make_golden.py``
+imports PyNOF with stub psi4/numba modules and records inputs and outputs).
+
+Array conventions (identical to the reference): ``C`` (N, N) with MO p in
+column p; ``b`` (N, N, Q) with Q fastest; ``I`` (N, N, N, N) with
+``I[m, n, s, l] = (mn|sl)``; ``H`` (N, N); ``n`` (P,); ``cj12``/``ck12`` (P, P).
+``p`` is any object with the ``pynof.param`` size attributes
+(nbf, nbf5, nbeta, nalpha, no1, noptorb, MSpin, HighSpin, RI, ...).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg
+
+
+# ----------------------------------------------------------------------------
+# A1 / A2: per-orbital J_i, K_i
+# ----------------------------------------------------------------------------
+def jkj_ri(C, b, P):
+    """J_q, K_q from the RI factor (``integrals.py:208-218`` JKj_RI).
+
+    T[q, n, l]  = sum_m C[m, q] b[m, n, l]
+    d[q, l]     = sum_n C[n, q] T[q, n, l]
+    J[q, m, n]  = sum_l d[q, l] b[m, n, l]
+    K[q, m, n]  = sum_l T[q, m, l] T[q, n, l]
+    """
+    N, _, Q = b.shape
+    Cp = C[:, :P]
+    T = (Cp.T @ b.reshape(N, N * Q)).reshape(P, N, Q)
+    d = np.einsum("nq,qnl->ql", Cp, T)
+    J = (d @ b.reshape(N * N, Q).T).reshape(P, N, N)
+    K = np.matmul(T, T.transpose(0, 2, 1))
+    return J, K
+
+
+def jkj_full(C, I, P):
+    """J_i, K_i from the 4-index tensor (``integrals.py:197-205`` JKj_Full).
+
+    D_i = C_i C_i^T;  J_i[m, n] = sum_sl D_i[s, l] (mn|sl);
+    K_i[m, s] = sum_nl D_i[n, l] (mn|sl).
+    """
+    N = I.shape[0]
+    Cp = C[:, :P]
+    D = np.einsum("mi,ni->imn", Cp, Cp)
+    J = (D.reshape(P, N * N) @ I.reshape(N * N, N * N).T).reshape(P, N, N)
+    # K needs (m,s) x (n,l): permute I to [m, s, n, l]
+    Iperm = I.transpose(0, 2, 1, 3).reshape(N * N, N * N)
+    K = (D.reshape(P, N * N) @ Iperm.T).reshape(P, N, N)
+    return J, K
+
+
+# ----------------------------------------------------------------------------
+# A3 / A4: MO-basis J_pq, K_pq, H_pp
+# ----------------------------------------------------------------------------
+def hcore_diag(C, H, P):
+    """H_core[p] = C_p^T H C_p (``integrals.py:345``, ``:361``)."""
+    Cp = C[:, :P]
+    return np.einsum("mp,mp->p", Cp, H @ Cp)
+
+
+def jkh_mo_ri(C, H, b, P):
+    """(pp|qq), (pq|pq), H_pp from b (``integrals.py:348-362`` JKH_MO_RI)."""
+    N, _, Q = b.shape
+    Cp = C[:, :P]
+    T = (Cp.T @ b.reshape(N, N * Q)).reshape(P, N, Q)          # [p, n, l]
+    bpq = np.matmul(Cp.T[None, :, :], T)                        # [p, q, l]
+    diag = bpq[np.arange(P), np.arange(P), :]                   # [p, l]
+    J_MO = diag @ diag.T
+    K_MO = np.einsum("pql,pql->pq", bpq, bpq)
+    return J_MO, K_MO, hcore_diag(C, H, P)
+
+
+def jkh_mo_full(C, H, I, P):
+    """(ii|jj), (ij|ij), H_ii from I (``integrals.py:332-345`` JKH_MO_Full)."""
+    N = I.shape[0]
+    Cp = C[:, :P]
+    D = np.einsum("mi,ni->imn", Cp, Cp).reshape(P, N * N)
+    J, K = jkj_full(C, I, P)
+    J_MO = J.reshape(P, N * N) @ D.T
+    K_MO = K.reshape(P, N * N) @ D.T
+    return J_MO, K_MO, hcore_diag(C, H, P)
+
+
+# ----------------------------------------------------------------------------
+# A5 / A6: MO integrals for the Lagrangian and computeLagrange2
+# ----------------------------------------------------------------------------
+def integrals_mo_ri(C, H, b, P):
+    """Hmat (N, P) and b_MO (N, P, Q) (``integrals.py:701-706``)."""
+    N, _, Q = b.shape
+    Hmat = C.T @ H @ C[:, :P]
+    Cp = C[:, :P]
+    # T[q, m, l] = sum_n C[n, q] b[m, n, l] = sum_n C[n, q] b[n, m, l] (b symmetric
+    # is NOT assumed here: contract the second index explicitly)
+    T = np.einsum("nq,mnl->qml", Cp, b)
+    bmo = np.einsum("ma,qml->aql", C, T)
+    return Hmat, bmo
+
+
+def integrals_mo_full(C, H, I, P):
+    """Hmat and I_MO[p, q, r, t] (``integrals.py:685-690``); p over N, q r t over P."""
+    Hmat = C.T @ H @ C[:, :P]
+    Cp = C[:, :P]
+    X = np.tensordot(I, Cp, axes=([3], [0]))        # m n s t
+    X = np.tensordot(X, Cp, axes=([2], [0]))        # m n t r
+    X = np.tensordot(X, Cp, axes=([1], [0]))        # m t r q
+    X = np.tensordot(X, C, axes=([0], [0]))         # t r q p
+    return Hmat, np.ascontiguousarray(X.transpose(3, 2, 1, 0))
+
+
+def _zero_diag(a):
+    np.fill_diagonal(a, 0.0)
+
+
+def lagrange2(n, cj12, ck12, C, H, I, b, p):
+    """elag (N, N) and Hmat (N, P) (``utils.py:262-382`` computeLagrange2).
+
+    Closed shell (MSpin == 0) only, as in the reference.  The diagonals of cj12
+    and ck12 are zeroed in place (``utils.py:269-270``).
+    """
+    N, P = p.nbf, p.nbf5
+    nb, na = p.nbeta, p.nalpha
+    _zero_diag(cj12)
+    _zero_diag(ck12)
+    elag = np.zeros((N, N))
+    if p.MSpin != 0:
+        # the reference assembles nothing for open shells (utils.py:272-274, :329-331)
+        Hmat = C.T @ H @ C[:, :P]
+        return elag, Hmat
+    if p.RI:
+        Hmat, bmo = integrals_mo_ri(C, H, b, P)
+        bbk = bmo[np.arange(P), np.arange(P), :]                      # [b, k] = bMO[b, b, k]
+        w = np.zeros_like(bbk)
+        w[:nb] += n[:nb, None] * bbk[:nb]
+        w[na:P] += n[na:P, None] * bbk[na:P]
+        w += cj12 @ bbk                                               # sum_q cj12[b,q] bMO[q,q,k]
+        elag[:, :P] += n[None, :] * Hmat[:, :P]
+        elag[:, :P] += np.einsum("abk,bk->ab", bmo, w)
+        Y = ck12[:, :, None] * bmo[:P]                                # [b, q, k]
+        elag[:, :P] -= bmo.reshape(N, -1) @ Y.reshape(P, -1).T
+    else:
+        Hmat, imo = integrals_mo_full(C, H, I, P)
+        ar = np.arange(P)
+        elag[:, :P] += n[None, :] * Hmat[:, :P]
+        diag3 = imo[:, ar, ar, ar]                                    # [a, b] = I_MO[a,b,b,b]
+        elag[:, :nb] += n[None, :nb] * diag3[:, :nb]
+        elag[:, na:P] += n[None, na:P] * diag3[:, na:P]
+        abqq = imo[:, :, ar, ar]                                      # [a, b, q]
+        elag[:, :P] += np.einsum("bq,abq->ab", cj12, abqq)
+        aqbq = np.einsum("aqbq->abq", imo)                           # [a, b, q] = I_MO[a,q,b,q]
+        elag[:, :P] -= np.einsum("bq,abq->ab", ck12, aqbq)
+    return elag, Hmat
+
+
+# ----------------------------------------------------------------------------
+# A8 / A7: generalized Fock, Lagrangian, energy
+# ----------------------------------------------------------------------------
+def fock_rc(J, K, n, H, cj12, ck12, p):
+    """F_i (P, N, N) closed shell (``utils.py:25-55`` computeF_RC_CPU).
+
+    Zeroes diag(cj12[ini:, ini:]) and diag(ck12[ini:, ini:]) in place.
+    """
+    P = p.nbf5
+    ini = p.no1 if p.no1 > 1 else 0
+    F = n[:, None, None] * H[None, :, :]
+    F = F.copy()
+    F[ini:p.nbeta] += n[ini:p.nbeta, None, None] * J[ini:p.nbeta]
+    F[p.nalpha:P] += n[p.nalpha:P, None, None] * J[p.nalpha:P]
+    _zero_diag(cj12[ini:, ini:])
+    _zero_diag(ck12[ini:, ini:])
+    N = J.shape[1]
+    F += (cj12 @ J.reshape(P, N * N)).reshape(P, N, N)
+    F -= (ck12 @ K.reshape(P, N * N)).reshape(P, N, N)
+    return F
+
+
+def lagrange(F, C, p):
+    """elag from F (``utils.py:249-259`` computeLagrange)."""
+    P, N, no = p.nbf5, p.nbf, p.noptorb
+    G = np.einsum("imn,ni->mi", F, C[:, :P])
+    elag = np.zeros((N, N))
+    elag[:no, :P] = (C[:, :no].T @ G)[:no, :P]
+    return elag
+
+
+def e_elec(H, C, n, elag, p):
+    """Electronic energy (``utils.py:385-402`` computeE_elec)."""
+    P, nb, na = p.nbf5, p.nbeta, p.nalpha
+    hd = hcore_diag(C, H, P)
+    E = np.trace(elag[:P, :P])
+    E += np.dot(n[:nb], hd[:nb])
+    if not p.HighSpin:
+        E += np.dot(n[nb:na], hd[nb:na])
+    else:
+        E += 0.5 * np.sum(hd[nb:na])
+    E += np.dot(n[na:P], hd[na:P])
+    return E
+
+
+def lagrange_convergency(elag):
+    """(sumdiff, maxdiff) of elag - elag^T (``utils.py:405-411``)."""
+    d = np.abs(elag - elag.T)
+    return d.sum(), d.max()
+
+
+def energy1r(C, n, H, I, b, cj12, ck12, p):
+    """E, elag, sumdiff, maxdiff (``utils.py:414-431`` ENERGY1r); closed shell."""
+    P = p.nbf5
+    if p.no1 == 0:
+        elag, Hmat = lagrange2(n, cj12, ck12, C, H, I, b, p)
+        E = np.trace(elag[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat)[:P])
+    else:
+        J, K = jkj_ri(C, b, P) if p.RI else jkj_full(C, I, P)
+        F = fock_rc(J, K, n, H, cj12, ck12, p)
+        elag = lagrange(F, C, p)
+        E = e_elec(H, C, n, elag, p)
+    s, m = lagrange_convergency(elag)
+    return E, elag, s, m
+
+
+# ----------------------------------------------------------------------------
+# A9 / A10: occupation-space energy and the orbital gradient
+# ----------------------------------------------------------------------------
+def calce(n, cj12, ck12, J_MO, K_MO, H_core, p):
+    """E(n) closed shell (``pnof.py:905-929`` calce, MSpin == 0)."""
+    P, nb, na = p.nbf5, p.nbeta, p.nalpha
+    dj = np.diagonal(J_MO)
+    E = 2.0 * np.dot(n, H_core) + np.dot(n[:nb], dj[:nb]) + np.dot(n[na:P], dj[na:P])
+    _zero_diag(cj12)
+    _zero_diag(ck12)
+    E += np.sum(cj12 * J_MO.T) - np.sum(ck12 * K_MO.T)
+    return E
+
+
+def orbital_gradient(elag, p):
+    """Packed 4 (elag - elag^T) over i < nbf5, j > i (``pnof.py:1114-1131``)."""
+    g = 4.0 * (elag - elag.T)
+    iu = np.triu_indices(p.nbf, 1)
+    keep = iu[0] < p.nbf5
+    return g[iu[0][keep], iu[1][keep]]
+
+
+def rotate_orbital(y, C, p):
+    """C expm(Y) with Y antisymmetric from packed y (``utils.py:550-565``)."""
+    N = p.nbf
+    Y = np.zeros((N, N))
+    iu = np.triu_indices(N, 1)
+    keep = iu[0] < p.nbf5
+    Y[iu[0][keep], iu[1][keep]] = y
+    Y -= Y.T
+    return C @ scipy.linalg.expm(Y)
+
+
+def eri_from_b(b):
+    """(mn|sl) = sum_Q b[m, n, Q] b[s, l, Q] (the exact RI identity)."""
+    N, _, Q = b.shape
+    B = b.reshape(N * N, Q)
+    return (B @ B.T).reshape(N, N, N, N)

@@ -1,0 +1,113 @@
+"""Drop-in mirror of PyNOF's GPU integral functions.
+
+Same names, argument order and return types as the functions PyNOF dispatches
+to when ``p.gpu`` is set (``pynof/integrals.py``), so that an installer can
+rebind them in the ``pynof`` namespace:
+
+* host inputs (``C``, ``H``, ``n``, ``cj12``, ``ck12``) are numpy float64 arrays
+  of any strides and are uploaded per call, like the reference's ``cp.array``;
+* ``b_mnl`` / ``I`` are device-resident (a float64 CUDA tensor, uploaded once
+  by :func:`upload_integrals`); numpy inputs are accepted and uploaded per call;
+* results come back as host numpy arrays, like the reference's ``.get()``,
+  except where the reference returns device arrays (``Integrals_MO_*_GPU``
+  return torch CUDA tensors where the reference returns cupy arrays).
+
+All arithmetic runs in ``libpynof_gb300.so``; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import ops
+
+
+def as_device(x) -> torch.Tensor:
+    if isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.float64 and x.is_contiguous():
+        return x
+    return ops.to_device(x)
+
+
+def to_host(*tensors):
+    """Copy device tensors into pinned host memory and return numpy arrays.
+
+    Pinned blocks come from torch's caching host allocator, so repeated calls
+    of the same size reuse the same page-locked memory once the caller drops
+    the previous result."""
+    outs = []
+    for t in tensors:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        outs.append(h)
+    torch.cuda.current_stream().synchronize()
+    res = tuple(h.numpy() for h in outs)
+    return res if len(res) > 1 else res[0]
+
+
+def upload_integrals(I, b_mnl, check_symmetry: bool = True):
+    """Device copies of the ERI tensor(s), the replacement for the ``cp.array``
+    upload at the end of ``compute_integrals`` (``pynof/integrals.py:51-53``)."""
+    dI = as_device(I) if I is not None and np.size(I) else I
+    db = None
+    if b_mnl is not None and np.size(b_mnl):
+        db = as_device(b_mnl)
+        if check_symmetry:
+            asym = ops.check_symmetric(db)
+            if asym != 0.0:
+                raise ValueError(f"b_mnl is not symmetric in (m, n) (max |b - b^T| = {asym:.3e}); "
+                                 "the RI kernels require the exact symmetry PyNOF's b_mnl has")
+    return dI, db
+
+
+# ---------------------------------------------------------------------------
+# A1  computeJKj
+# ---------------------------------------------------------------------------
+def JKj_RI_GPU(C, b_mnl, p):
+    """J, K (nbf5, nbf, nbf) -- ``pynof/integrals.py:234-245``."""
+    J, K = ops.jkj_ri(as_device(C), as_device(b_mnl), p.nbf5)
+    return to_host(J, K)
+
+
+def computeJKj(C, I, b_mnl, p):
+    """Dispatcher of ``pynof/integrals.py:172-191`` for the device path."""
+    if p.RI:
+        return JKj_RI_GPU(C, b_mnl, p)
+    from . import integrals_full
+
+    return integrals_full.JKj_Full_GPU(C, I, p)
+
+
+# ---------------------------------------------------------------------------
+# A3  computeJKH_MO
+# ---------------------------------------------------------------------------
+def JKH_MO_RI_GPU(C, H, b_mnl, p):
+    """J_MO, K_MO (nbf5, nbf5), H_core (nbf5,) -- ``pynof/integrals.py:383-399``."""
+    a, b, c = ops.jkh_mo_ri(as_device(C), as_device(H), as_device(b_mnl), p.nbf5)
+    return to_host(a, b, c)
+
+
+def computeJKH_MO(C, H, I, b_mnl, p):
+    """Dispatcher of ``pynof/integrals.py:307-326`` for the device path."""
+    if p.RI:
+        return JKH_MO_RI_GPU(C, H, b_mnl, p)
+    from . import integrals_full
+
+    return integrals_full.JKH_MO_Full_GPU(C, H, I, p)
+
+
+# ---------------------------------------------------------------------------
+# A5  JKH_MO_tmp / Integrals_MO_RI
+# ---------------------------------------------------------------------------
+def Integrals_MO_RI_GPU(C, H, b_mnl, p):
+    """H_mat (nbf, nbf5), b_MO (nbf, nbf5, naux) as CUDA tensors --
+    ``pynof/integrals.py:709-714`` (which returns device arrays too)."""
+    return ops.mo_ri(as_device(C), as_device(H), as_device(b_mnl), p.nbf5)
+
+
+def JKH_MO_tmp(C, H, I, b_mnl, p):
+    """Dispatcher of ``pynof/integrals.py:665-682`` for the device path."""
+    if p.RI:
+        return Integrals_MO_RI_GPU(C, H, b_mnl, p)
+    from . import integrals_full
+
+    return integrals_full.Integrals_MO_Full_GPU(C, H, I, p)

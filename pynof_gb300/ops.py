@@ -1,0 +1,153 @@
+"""Device-resident operations over torch CUDA tensors.
+
+Each function allocates its outputs with torch, takes scratch from a per-device
+workspace pool, and calls one C-ABI entry point of ``libpynof_gb300.so`` on
+torch's current CUDA stream.  torch supplies memory and streams only; all
+arithmetic is in the library's CUDA kernels.  Inputs must already be float64
+CUDA tensors (``to_device`` converts numpy arrays).
+"""
+from __future__ import annotations
+
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_F64 = torch.float64
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(device: torch.device | None = None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def to_device(x, device=None) -> torch.Tensor:
+    """float64, C-contiguous CUDA tensor view/copy of ``x`` (numpy or torch)."""
+    device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if isinstance(x, torch.Tensor):
+        t = x.to(device=device, dtype=_F64)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(x, dtype=np.float64))).to(device)
+    return t.contiguous()
+
+
+def _require(t: torch.Tensor, shape, name: str) -> None:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != _F64:
+        raise TypeError(f"{name} must be float64, got {t.dtype}")
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+class WorkspacePool:
+    """One growing scratch buffer per (device, stream); reused across calls.
+
+    Calls on the same stream are ordered, so reuse is safe; different streams
+    get different buffers.
+    """
+
+    def __init__(self):
+        self._bufs: dict[tuple[int, int], torch.Tensor] = {}
+        self._lock = threading.Lock()
+
+    def get(self, nbytes: int, device: torch.device) -> torch.Tensor:
+        key = (device.index if device.index is not None else torch.cuda.current_device(), _stream(device))
+        with self._lock:
+            buf = self._bufs.get(key)
+            if buf is None or buf.numel() < nbytes:
+                buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
+                self._bufs[key] = buf
+            return buf
+
+    def clear(self) -> None:
+        with self._lock:
+            self._bufs.clear()
+
+
+POOL = WorkspacePool()
+
+
+def _ws(query: str, *sizes, device) -> tuple[int, int]:
+    n = _lib.query(query, *sizes)
+    buf = POOL.get(n, device)
+    return buf.data_ptr(), buf.numel()
+
+
+# ----------------------------------------------------------------------------
+def check_symmetric(b: torch.Tensor) -> float:
+    """max |b[m, n, l] - b[n, m, l]| (the RI kernels require exact symmetry)."""
+    N, N2, Q = b.shape
+    _require(b, (N, N, Q), "b")
+    out = torch.empty(1, dtype=_F64, device=b.device)
+    _lib.call("gb_check_symmetric_f64", _ptr(b), N, Q, _ptr(out), _stream(b.device))
+    return float(out.item())
+
+
+def jkj_ri(C: torch.Tensor, b: torch.Tensor, nbf5: int):
+    """J, K (nbf5, nbf, nbf) from the RI factor (A1, computeJKj)."""
+    N, _, Q = b.shape
+    _require(C, (N, N), "C")
+    _require(b, (N, N, Q), "b")
+    J = torch.empty((nbf5, N, N), dtype=_F64, device=b.device)
+    K = torch.empty((nbf5, N, N), dtype=_F64, device=b.device)
+    wp, wn = _ws("gb_jkj_ri_workspace_f64", N, nbf5, Q, device=b.device)
+    _lib.call("gb_jkj_ri_f64", _ptr(C), _ptr(b), N, nbf5, Q, _ptr(J), _ptr(K), wp, wn, _stream(b.device))
+    return J, K
+
+
+def jkh_mo_ri(C: torch.Tensor, H: torch.Tensor, b: torch.Tensor, nbf5: int):
+    """J_MO, K_MO (nbf5, nbf5), H_core (nbf5,) from the RI factor (A3)."""
+    N, _, Q = b.shape
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(b, (N, N, Q), "b")
+    dev = b.device
+    J_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    K_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    H_core = torch.empty((nbf5,), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_jkh_mo_ri_workspace_f64", N, nbf5, Q, device=dev)
+    _lib.call("gb_jkh_mo_ri_f64", _ptr(C), _ptr(H), _ptr(b), N, nbf5, Q, _ptr(J_MO), _ptr(K_MO), _ptr(H_core),
+              wp, wn, _stream(dev))
+    return J_MO, K_MO, H_core
+
+
+def mo_ri(C: torch.Tensor, H: torch.Tensor, b: torch.Tensor, nbf5: int):
+    """Hmat (nbf, nbf5) and bMO (nbf, nbf5, naux) (A5, Integrals_MO_RI)."""
+    N, _, Q = b.shape
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(b, (N, N, Q), "b")
+    dev = b.device
+    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    bMO = torch.empty((N, nbf5, Q), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_mo_ri_workspace_f64", N, nbf5, Q, device=dev)
+    _lib.call("gb_mo_ri_f64", _ptr(C), _ptr(H), _ptr(b), N, nbf5, Q, _ptr(Hmat), _ptr(bMO), wp, wn, _stream(dev))
+    return Hmat, bMO
+
+
+def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
+    """elag (nbf, nbf) and Hmat (nbf, nbf5) (A5, computeLagrange2 RI closed shell).
+
+    The diagonals of cj12 / ck12 are ignored (treated as zero)."""
+    N, _, Q = b.shape
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(b, (N, N, Q), "b")
+    _require(n, (nbf5,), "n")
+    _require(cj12, (nbf5, nbf5), "cj12")
+    _require(ck12, (nbf5, nbf5), "ck12")
+    dev = b.device
+    elag = torch.empty((N, N), dtype=_F64, device=dev)
+    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_lagrange2_ri_workspace_f64", N, nbf5, Q, device=dev)
+    _lib.call("gb_lagrange2_ri_f64", _ptr(C), _ptr(H), _ptr(b), _ptr(n), _ptr(cj12), _ptr(ck12), N, nbf5, Q,
+              nbeta, nalpha, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
+    return elag, Hmat

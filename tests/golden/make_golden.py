@@ -1,0 +1,206 @@
+"""Generate the golden fixtures by running PyNOF's own functions.
+
+This script is the only place that executes the reference.  It imports PyNOF
+from a source checkout (``--ref``, default ``/root/reference/src``) with two
+stub modules standing in for packages that are not installed and that the hot
+path does not need:
+
+* ``psi4``: an empty module (only referenced at import time and by functions
+  off the path -- integral generation, basis sets, HF guesses);
+* ``numba``: ``njit``/``jit`` as identity decorators and ``prange = range``, so
+  the ``*_jit`` variants run as plain Python with the same arithmetic.
+
+``sys.pycache_prefix`` points at a scratch directory so that only the ``.py``
+sources are executed.
+
+For each case it draws the seeded synthetic inputs
+(``pynof_gb300.synthetic.make_inputs``), calls the reference functions on
+copies of them, cross-checks the numpy and ``*_jit`` variants against each
+other, and writes inputs plus outputs to ``tests/golden/<case>.npz``.
+
+Run:  python tests/golden/make_golden.py [--ref PATH]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+from pynof_gb300 import synthetic  # noqa: E402
+
+CASES = {
+    # name: (workload, seed, run_full_eri, run_jit_variants)
+    "c1": ("c1", 0, True, True),
+    "water": ("water", 0, True, False),
+    "ragged": ("ragged", 3, False, False),
+}
+
+
+def import_reference(ref_src):
+    sys.pycache_prefix = tempfile.mkdtemp(prefix="pycache_ref_")
+    psi4 = types.ModuleType("psi4")
+    psi4.core = types.ModuleType("psi4.core")
+    sys.modules["psi4"] = psi4
+    sys.modules["psi4.core"] = psi4.core
+    numba = types.ModuleType("numba")
+
+    def njit(*args, **kwargs):
+        if len(args) == 1 and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda f: f
+
+    numba.njit = njit
+    numba.jit = njit
+    numba.prange = range
+    sys.modules["numba"] = numba
+    sys.path.insert(0, ref_src)
+    import pynof  # noqa: F401
+
+    return pynof
+
+
+def make_param(st: synthetic.Structure, **over):
+    keys = ["nbf", "nbfaux", "ndoc", "ncwo", "no1", "nsoc", "MSpin", "HighSpin", "RI", "ipnof",
+            "occ_method", "nbeta", "nalpha", "ndns", "nac", "nbf5", "no0", "noptorb", "nv", "nvar",
+            "maxloop", "alpha"]
+    d = {k: getattr(st, k) for k in keys}
+    d.update(gpu=False, jit=False, ista=0, lamb=0.0, freeze_occ=False, occupation_optimizer="CG")
+    d.update(over)
+    return types.SimpleNamespace(**d)
+
+
+def nrel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def run_case(pynof, name, workload, seed, full, jit):
+    st = synthetic.structure(workload)
+    b, C, H, n = synthetic.make_inputs(st, seed)
+    p = make_param(st)
+    P = st.nbf5
+    out = dict(b=b, C=C, H=H, n=n)
+    checks = {}
+
+    # occupation parameters (softmax encoding) and GNOF coefficients
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    # compute_gammas_softmax (utils.py:680-689) indexes with stride ncwo and
+    # overruns its array when ndoc < ncwo; every entry it writes has the same
+    # value, so the guess is built directly here.
+    g0 = np.log(max(0.001 / st.ncwo, 1e-16)) - np.log(0.999)
+    gamma = np.full(st.nv, g0) + 0.3 * rng.standard_normal(st.nv)
+    n_soft, dn = pynof.ocupacion_softmax(gamma, st.no1, st.ndoc, st.nalpha, st.nv, P, st.ndns, st.ncwo,
+                                         st.HighSpin)
+    cj12, ck12 = pynof.PNOFi_selector(n_soft, p)
+    Dcj, Dck = pynof.der_PNOFi_selector(n_soft, dn, p)
+    out.update(gamma=gamma, n_soft=n_soft, dn_soft=dn, cj12=cj12.copy(), ck12=ck12.copy(),
+               Dcj12=Dcj, Dck12=Dck)
+
+    # A1 computeJKj (RI)
+    J, K = pynof.computeJKj(C, [], b, p)
+    out.update(J_ri=J, K_ri=K)
+    if jit:
+        Jj, Kj = pynof.JKj_RI_jit(C, b, st.nbf, P, st.nbfaux)
+        checks["JKj_RI_jit_vs_numpy"] = max(nrel(Jj, J), nrel(Kj, K))
+
+    # A3 computeJKH_MO (RI)
+    J_MO, K_MO, H_core = pynof.computeJKH_MO(C, H, [], b, p)
+    out.update(J_MO_ri=J_MO, K_MO_ri=K_MO, H_core=H_core)
+    if jit:
+        a, bb, c = pynof.JKH_MO_RI_jit(C, H, b, st.nbf, P, st.nbfaux)
+        checks["JKH_MO_RI_jit_vs_numpy"] = max(nrel(a, J_MO), nrel(bb, K_MO), nrel(c, H_core))
+
+    # A5 Integrals_MO_RI + computeLagrange2 (RI)
+    Hmat, bmo = pynof.Integrals_MO_RI_CPU(C, H, b, p)
+    out.update(Hmat=Hmat, b_MO=bmo)
+    elag2, Hmat2 = pynof.computeLagrange2(n_soft, cj12.copy(), ck12.copy(), C, H, [], b, p)
+    out.update(elag2_ri=elag2)
+
+    # A7 ENERGY1r (no1 == 0 route)
+    E, elag, sd, md = pynof.ENERGY1r(C, n_soft, H, [], b, cj12.copy(), ck12.copy(), p)
+    out.update(E1r=np.array(E), elag1r=elag, sumdiff1r=np.array(sd), maxdiff1r=np.array(md))
+
+    # A8 generalized Fock route on the recipe occupations
+    F = pynof.computeF_RC_CPU(J, K, n_soft, H, cj12.copy(), ck12.copy(), p)
+    elagF = pynof.computeLagrange(F, C, p)
+    EF = pynof.computeE_elec(H, C, n_soft, elagF, p)
+    out.update(F_rc=F, elag_F=elagF, E_F=np.array(EF))
+    checks["E_fock_route_vs_lagrange2_route"] = abs(EF - E)
+
+    # ENERGY1r with no1 = nbeta (the HF-like route hfidr takes, minimization.py:9-19)
+    ph = make_param(st, no1=st.nbeta)
+    nh = np.zeros(P)
+    nh[: st.nbeta] = 1.0
+    cjh = 2 * np.outer(nh, nh)
+    ckh = np.outer(nh, nh)
+    Eh, elagh, sdh, mdh = pynof.ENERGY1r(C, nh, H, [], b, cjh, ckh, ph)
+    out.update(E1r_hf=np.array(Eh), elag1r_hf=elagh)
+
+    # A9 occupation energy and gradient
+    Ec = pynof.calce(n_soft, cj12.copy(), ck12.copy(), J_MO, K_MO, H_core, p)
+    Eo = pynof.calcocce(gamma, J_MO, K_MO, H_core, p)
+    go = pynof.calcoccg(gamma, J_MO, K_MO, H_core, p)
+    out.update(E_calce=np.array(Ec), E_calcocce=np.array(Eo), g_occ=go)
+
+    # A10 / A11 orbital gradient, orbital energy, rotation
+    y0 = np.zeros(st.nvar)
+    g_orb = pynof.calcorbg(y0, n_soft, cj12.copy(), ck12.copy(), C, H, [], b, p)
+    y = 0.01 * rng.standard_normal(st.nvar)
+    Cr = pynof.rotate_orbital(y, C, p)
+    Eorb = pynof.calcorbe(y, n_soft, cj12.copy(), ck12.copy(), C, H, [], b, p)
+    out.update(g_orb=g_orb, y=y, C_rot=Cr, E_orb=np.array(Eorb))
+
+    # order_occupations_softmax (guess.py:77-106)
+    Cs, gs = pynof.order_occupations_softmax(C, gamma, H, [], b, p)
+    out.update(C_sorted=Cs, gamma_sorted=gs)
+
+    if full:
+        I = np.einsum("mnQ,slQ->mnsl", b, b, optimize=True)
+        pf = make_param(st, RI=False)
+        Jf, Kf = pynof.computeJKj(C, I, [], pf)
+        out.update(J_full=Jf, K_full=Kf)
+        checks["JKj_full_vs_ri"] = max(nrel(Jf, J), nrel(Kf, K))
+        a, bb, c = pynof.computeJKH_MO(C, H, I, [], pf)
+        out.update(J_MO_full=a, K_MO_full=bb)
+        checks["JKH_MO_full_vs_ri"] = max(nrel(a, J_MO), nrel(bb, K_MO))
+        ef, _ = pynof.computeLagrange2(n_soft, cj12.copy(), ck12.copy(), C, H, I, [], pf)
+        out.update(elag2_full=ef)
+        checks["lagrange2_full_vs_ri"] = nrel(ef, elag2)
+        if jit:
+            Jj, Kj = pynof.JKj_Full_jit(C, I, st.nbf, P)
+            checks["JKj_Full_jit_vs_numpy"] = max(nrel(Jj, Jf), nrel(Kj, Kf))
+            a2, b2, c2 = pynof.JKH_MO_Full_jit(C, H, I, st.nbf, P)
+            checks["JKH_MO_Full_jit_vs_numpy"] = max(nrel(a2, a), nrel(b2, bb))
+
+    meta = dict(case=name, workload=workload, seed=seed, sizes=synthetic.WORKLOADS[workload],
+                numpy=np.__version__, checks=checks)
+    return out, meta
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    pynof = import_reference(args.ref)
+    allmeta = {}
+    for name, (workload, seed, full, jit) in CASES.items():
+        out, meta = run_case(pynof, name, workload, seed, full, jit)
+        np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
+        allmeta[name] = meta
+        print(name, json.dumps(meta["checks"]))
+    with open(os.path.join(args.out, "golden_meta.json"), "w") as f:
+        json.dump(allmeta, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,56 @@
+"""The C-ABI library builds, loads and exports every symbol the header declares.
+
+No GPU needed: only size queries (pure host arithmetic) are called.
+"""
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "pynof_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pynof_gb300 import _lib, build
+
+    build.build()
+    return _lib.load()
+
+
+def test_header_symbols_exported(lib):
+    from pynof_gb300 import _lib
+
+    names = declared_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} missing from the ctypes signature table"
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (gb_\w+)", out))
+    assert set(names) <= exported
+    assert set(_lib.SIGNATURES) <= exported
+
+
+def test_workspace_queries(lib):
+    from pynof_gb300 import _lib
+
+    N, P, Q = 600, 300, 2400
+    ws = _lib.query("gb_jkj_ri_workspace_f64", N, P, Q)
+    assert ws >= P * N * Q * 8 + P * Q * 8
+    assert ws % 256 == 0
+    assert _lib.query("gb_lagrange2_ri_workspace_f64", N, P, Q) >= 2 * N * P * Q * 8
+
+
+def test_version_and_error(lib):
+    assert lib.gb_version() >= 100
+    assert isinstance(lib.gb_last_error(), bytes)
