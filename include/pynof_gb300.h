@@ -72,6 +72,20 @@ size_t gb_jkj_ri_workspace_f64(int nbf, int nbf5, int naux);
 int gb_jkj_ri_f64(const double* C, const double* b, int nbf, int nbf5, int naux, double* J, double* K,
                   void* workspace, size_t workspace_bytes, void* stream);
 
+/* Same build as gb_jkj_ri_f64 for callers that cannot allocate device memory
+ * (their HBM is owned by another allocator or a fixed arena, or they run in a
+ * loop where cudaMalloc/cudaFree would synchronise the device).  No counterpart
+ * in the reference: PyNOF always lets cupy allocate.  Scratch comes from a
+ * built-in device array of GB_NOALLOC_SCRATCH_BYTES, reserved on every GPU that
+ * loads this library until the process exits; problems whose workspace
+ * (gb_jkj_ri_workspace_f64) exceeds it are rejected with GB_ERR_WORKSPACE.
+ * The first call on a device looks the array's address up (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised on one stream. */
+#define GB_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int gb_jkj_ri_noalloc_f64(const double* C, const double* b, int nbf, int nbf5, int naux, double* J, double* K,
+                          void* stream);
+
 /* ------------------------------------------------------------------------
  * A3  computeJKH_MO, RI.  Replaces JKH_MO_RI_GPU (pynof/integrals.py:383-399),
  *     dispatched from computeJKH_MO (pynof/integrals.py:307-326).

@@ -38,6 +38,7 @@ SIGNATURES = {
     "gb_check_symmetric_f64": (_I, [_P, _I, _I, _P, _P]),
     "gb_jkj_ri_workspace_f64": (_Z, [_I, _I, _I]),
     "gb_jkj_ri_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_jkj_ri_noalloc_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _P]),
     "gb_jkh_mo_ri_workspace_f64": (_Z, [_I, _I, _I]),
     "gb_jkh_mo_ri_f64": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _Z, _P]),
     "gb_mo_ri_workspace_f64": (_Z, [_I, _I, _I]),
