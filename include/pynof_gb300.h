@@ -118,6 +118,43 @@ int gb_lagrange2_ri_f64(const double* C, const double* H, const double* b, const
                         int nalpha, double* elag, double* Hmat, void* workspace, size_t workspace_bytes,
                         void* stream);
 
+/* ========================================================================
+ * Split-product ("mixed") path on the tcgen05 tensor cores.
+ *
+ * FP64 operands are cut into nslices (1..6) balanced base-128 bf16 digit
+ * slices with a power-of-two exponent per row; the slice products with
+ * s + t <= nslices + 1 run as bf16 tcgen05 MMAs with FP32 accumulation in
+ * TMEM, the leading product groups accumulated exactly.  nslices = 6 agrees
+ * with FP64 to ~1e-12 normwise; nslices = 2 is the three-product bf16x3 split
+ * (~1e-5).  Device status of these kernels: gb_device_status.
+ * ====================================================================== */
+
+/* Status word of the tensor-core kernels on the current device: 0, or
+ * GB_ERR_TIMEOUT when one of their bounded waits gave up.  Synchronises the
+ * device; reset != 0 clears the word. */
+int gb_device_status(int reset, int* status);
+
+/* Generic FP64-accurate GEMM on the tensor cores: C = A B^T with row-major
+ * A [M][K], B [N][K], C [M][N].  No counterpart in the reference (PyNOF's
+ * GEMMs go through numpy / cupy). */
+size_t gb_dgemm_mixed_workspace(int M, int N, int K, int nslices);
+int gb_dgemm_mixed(const double* A, const double* B, int M, int N, int K, int nslices, double* C, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* Slice the RI factor once (the resident operand of every build):
+ * replaces the device copy made at the end of compute_integrals
+ * (pynof/integrals.py:51-53) for the mixed path.  prep must hold
+ * gb_ri_prepare_bytes_mixed bytes and stays valid while b is unchanged. */
+size_t gb_ri_prepare_bytes_mixed(int nbf, int naux, int nslices);
+int gb_ri_prepare_mixed(const double* b, int nbf, int naux, int nslices, void* prep, size_t prep_bytes,
+                        void* stream);
+
+/* A1  computeJKj, RI, on the tensor cores (same outputs as gb_jkj_ri_f64).
+ *     Replaces JKj_RI_GPU (pynof/integrals.py:234-245). */
+size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
+int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
+                    double* K, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

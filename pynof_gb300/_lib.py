@@ -45,6 +45,13 @@ SIGNATURES = {
     "gb_mo_ri_f64": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P, _Z, _P]),
     "gb_lagrange2_ri_workspace_f64": (_Z, [_I, _I, _I]),
     "gb_lagrange2_ri_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
+    "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
+    "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_ri_prepare_bytes_mixed": (_Z, [_I, _I, _I]),
+    "gb_ri_prepare_mixed": (_I, [_P, _I, _I, _I, _P, _Z, _P]),
+    "gb_jkj_ri_workspace_mixed": (_Z, [_I, _I, _I, _I]),
+    "gb_jkj_ri_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
 }
 
 _lock = threading.Lock()
@@ -93,6 +100,13 @@ def call(name: str, *args) -> None:
 
 def query(name: str, *args) -> int:
     return int(getattr(load(), name)(*args))
+
+
+def device_status(reset: bool = True) -> int:
+    """Status word of the tensor-core kernels (0 = ok); synchronises the device."""
+    v = _c.c_int(0)
+    call("gb_device_status", 1 if reset else 0, _c.byref(v))
+    return int(v.value)
 
 
 def profile_start() -> None:

@@ -1,0 +1,43 @@
+// Split-product FP64 GEMM on the tcgen05 tensor cores (bf16 digit slices).
+//
+// C[b](i, j) = (-1)^negate * sum_k A[b](i, k) B[b](j, k)
+// with A, B given as digit slices (slice.cuh).  The slice products are grouped
+// by g = s + t (uniform weight 2^(-7 g) inside a group).  Groups g <= 4 are the
+// leading ones: they accumulate in FP32 TMEM over chunks of 192 k, where every
+// partial sum is an integer multiple of 2^(-7 g) below 2^22 units and hence
+// exact, and are drained into per-element int64 accumulators after each
+// chunk.  Groups 5..S+1 (2^(-21) and less relative to the leading group)
+// accumulate together in one FP32 accumulator over the whole K.  The epilogue
+// assembles the FP64 result from the int64 and FP32 parts with integer
+// arithmetic only.  Products with s + t > S + 1 are not formed.
+//
+// Accuracy: each element carries the slicing error (|x| 2^(-7 S - 1) per
+// operand element relative to its row's power-of-two bound) plus the
+// truncation of the product triangle; with S = 6 the result agrees with FP64
+// to ~1e-12 normwise on the path's operands.  S = 2 is the classic
+// three-product bf16x3 split.
+#pragma once
+
+#include "gemm_f64.cuh"
+#include "slice.cuh"
+
+namespace gb {
+
+struct OzGemm {
+  int M, N, K, batch, S;
+  double* C;
+  long long c_sb;
+  Index2 c_r, c_c;
+  int sym, pair_n;
+  int negate;
+  const char* tag = "ozaki_tc";
+};
+
+// A: rows are the M index; B: rows are the N index; both K-major slices.
+int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaStream_t stream);
+
+// Device status word of the tensor-core kernels (0 = ok, GB_ERR_TIMEOUT when a
+// bounded wait gave up).  Reading synchronises the current device.
+int ozaki_status(int reset, int* out);
+
+}  // namespace gb

@@ -1,0 +1,201 @@
+// Split-product (tcgen05) RI path: computeJKj with FP64-accurate results from
+// bf16 digit slices.  See ozaki_tc.cuh for the arithmetic.
+//
+// The RI factor is sliced once ("prepared") into two K-major digit copies:
+//   bT[j = (n, l)][m]  (K = m, for the half transform T = C_p^T b)
+//   bJ[j = (m, n)][l]  (K = l, for J = d b^T)
+// and stays resident across builds, like b itself in PyNOF's GPU path.
+#include "ozaki_tc.cuh"
+#include "ri_kernels.cuh"
+#include "slice.cuh"
+
+using namespace gb;
+
+namespace {
+
+struct Prepared {
+  SlicedDesc bT, bJ;
+};
+
+template <class C>
+void prepared_layout(C& c, int N, int Q, int S, Prepared* out) {
+  const int kN = slice_kpad(N), kQ = slice_kpad(Q);
+  auto* tp = c.template take<__nv_bfloat16>((size_t)S * N * Q * kN);
+  auto* te = c.template take<int>((size_t)N * Q);
+  auto* jp = c.template take<__nv_bfloat16>((size_t)S * N * N * kQ);
+  auto* je = c.template take<int>((size_t)N * N);
+  if (out) {
+    out->bT = SlicedDesc{tp, te, 1, N * Q, N, kN, S};
+    out->bJ = SlicedDesc{jp, je, 1, N * N, Q, kQ, S};
+  }
+}
+
+struct SizeCarve {
+  size_t used = 0;
+  template <class T>
+  T* take(size_t n) {
+    used += align256(n * sizeof(T));
+    return nullptr;
+  }
+};
+
+int check_mixed(int N, int P, int Q, int S) {
+  GB_REQUIRE(N > 0 && P > 0 && Q > 0 && P <= N, GB_ERR_BAD_SHAPE,
+             "invalid sizes nbf=%d nbf5=%d naux=%d (need 0 < nbf5 <= nbf, naux > 0)", N, P, Q);
+  GB_REQUIRE(S >= 1 && S <= 6, GB_ERR_INVALID_ARG, "nslices=%d outside [1, 6]", S);
+  GB_REQUIRE((long long)N * Q < 2147483647LL && (long long)N * N < 2147483647LL, GB_ERR_BAD_SHAPE,
+             "sizes too large");
+  return GB_OK;
+}
+
+struct JkjMixedWs {
+  SlicedDesc A, d, T;
+  double* Tf;
+  double* dv;
+};
+
+template <class C>
+void jkj_mixed_layout(C& c, int N, int P, int Q, int S, JkjMixedWs* w) {
+  const int kN = slice_kpad(N), kQ = slice_kpad(Q);
+  auto* ap = c.template take<__nv_bfloat16>((size_t)S * P * kN);
+  auto* ae = c.template take<int>((size_t)P);
+  auto* tf = c.template take<double>((size_t)P * N * Q);
+  auto* dv = c.template take<double>((size_t)P * Q);
+  auto* dp = c.template take<__nv_bfloat16>((size_t)S * P * kQ);
+  auto* de = c.template take<int>((size_t)P);
+  auto* tp = c.template take<__nv_bfloat16>((size_t)P * S * N * kQ);
+  auto* te = c.template take<int>((size_t)P * N);
+  if (w) {
+    w->A = SlicedDesc{ap, ae, 1, P, N, kN, S};
+    w->Tf = tf;
+    w->dv = dv;
+    w->d = SlicedDesc{dp, de, 1, P, Q, kQ, S};
+    w->T = SlicedDesc{tp, te, P, N, Q, kQ, S};
+  }
+}
+
+}  // namespace
+
+extern "C" size_t gb_ri_prepare_bytes_mixed(int nbf, int naux, int nslices) {
+  SizeCarve c;
+  prepared_layout(c, nbf, naux, nslices, nullptr);
+  return c.used;
+}
+
+extern "C" int gb_ri_prepare_mixed(const double* b, int nbf, int naux, int nslices, void* prep, size_t prep_bytes,
+                                   void* stream) {
+  clear_error();
+  const int N = nbf, Q = naux, S = nslices;
+  GB_TRY(check_mixed(N, 1, Q, S));
+  GB_REQUIRE(b && prep, GB_ERR_INVALID_ARG, "gb_ri_prepare_mixed: null pointer");
+  GB_REQUIRE(prep_bytes >= gb_ri_prepare_bytes_mixed(N, Q, S), GB_ERR_WORKSPACE,
+             "gb_ri_prepare_mixed: buffer too small (%zu < %zu)", prep_bytes, gb_ri_prepare_bytes_mixed(N, Q, S));
+  Carve c(prep, prep_bytes);
+  Prepared pr;
+  prepared_layout(c, N, Q, S, &pr);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // bT rows j = n*Q + l over K = m: element b[m][j]   (rows are the unit stride)
+  GB_TRY(slice_operand(SliceSrc{b, 0, lin(1), lin((long long)N * Q), false}, pr.bT, s));
+  // bJ rows j = m*N + n over K = l: element b[j][l]  (K is the unit stride)
+  GB_TRY(slice_operand(SliceSrc{b, 0, lin(Q), lin(1), true}, pr.bJ, s));
+  return GB_OK;
+}
+
+extern "C" size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices) {
+  SizeCarve c;
+  jkj_mixed_layout(c, nbf, nbf5, naux, nslices, nullptr);
+  return c.used;
+}
+
+extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
+                               double* K, void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(check_mixed(N, P, Q, S));
+  GB_REQUIRE(C && prep && J && K, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_jkj_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "gb_jkj_ri_mixed: workspace too small (%zu < %zu)", workspace_bytes,
+             gb_jkj_ri_workspace_mixed(N, P, Q, S));
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  // A rows q over K = m: element C[m][q]
+  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
+  // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
+  OzGemm gt{};
+  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = S;
+  gt.C = w.Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
+  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
+  GB_TRY(ozaki_gemm(w.A, pr.bT, gt, s));
+  GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s));
+  // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
+  GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
+  OzGemm gj{};
+  gj.M = P; gj.N = N * N; gj.K = Q; gj.batch = 1; gj.S = S;
+  gj.C = J; gj.c_sb = 0; gj.c_r = lin((long long)N * N); gj.c_c = lin(1);
+  gj.sym = SYM_PAIRCOL; gj.pair_n = N; gj.tag = "ozaki_tc:J";
+  GB_TRY(ozaki_gemm(w.d, pr.bJ, gj, s));
+  // K[q] = T_q T_q^T
+  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s));
+  OzGemm gk{};
+  gk.M = N; gk.N = N; gk.K = Q; gk.batch = P; gk.S = S;
+  gk.C = K; gk.c_sb = (long long)N * N; gk.c_r = lin(N); gk.c_c = lin(1);
+  gk.sym = SYM_ROWCOL; gk.tag = "ozaki_tc:K";
+  GB_TRY(ozaki_gemm(w.T, w.T, gk, s));
+  return GB_OK;
+}
+
+extern "C" int gb_device_status(int reset, int* status) {
+  clear_error();
+  GB_REQUIRE(status, GB_ERR_INVALID_ARG, "gb_device_status: null pointer");
+  return ozaki_status(reset, status);
+}
+
+// ---------------------------------------------------------------------------
+// Generic FP64-accurate GEMM on the tensor cores: C = A B^T (row-major A [M][K],
+// B [N][K], C [M][N]).
+// ---------------------------------------------------------------------------
+namespace {
+template <class Cv>
+void dgemm_layout(Cv& c, int M, int N, int K, int S, SlicedDesc* a, SlicedDesc* b) {
+  const int kp = slice_kpad(K);
+  auto* ap = c.template take<__nv_bfloat16>((size_t)S * M * kp);
+  auto* ae = c.template take<int>((size_t)M);
+  auto* bp = c.template take<__nv_bfloat16>((size_t)S * N * kp);
+  auto* be = c.template take<int>((size_t)N);
+  if (a) *a = SlicedDesc{ap, ae, 1, M, K, kp, S};
+  if (b) *b = SlicedDesc{bp, be, 1, N, K, kp, S};
+}
+}  // namespace
+
+extern "C" size_t gb_dgemm_mixed_workspace(int M, int N, int K, int nslices) {
+  SizeCarve c;
+  dgemm_layout(c, M, N, K, nslices, nullptr, nullptr);
+  return c.used;
+}
+
+extern "C" int gb_dgemm_mixed(const double* A, const double* B, int M, int N, int K, int nslices, double* C,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  GB_REQUIRE(M > 0 && N > 0 && K > 0, GB_ERR_BAD_SHAPE, "gb_dgemm_mixed: bad sizes M=%d N=%d K=%d", M, N, K);
+  GB_REQUIRE(nslices >= 1 && nslices <= 6, GB_ERR_INVALID_ARG, "gb_dgemm_mixed: nslices=%d outside [1, 6]", nslices);
+  GB_REQUIRE(A && B && C, GB_ERR_INVALID_ARG, "gb_dgemm_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_dgemm_mixed_workspace(M, N, K, nslices), GB_ERR_WORKSPACE,
+             "gb_dgemm_mixed: workspace too small");
+  Carve wc(workspace, workspace_bytes);
+  SlicedDesc sa, sb;
+  dgemm_layout(wc, M, N, K, nslices, &sa, &sb);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GB_TRY(slice_operand(SliceSrc{A, 0, lin(K), lin(1), true}, sa, s));
+  GB_TRY(slice_operand(SliceSrc{B, 0, lin(K), lin(1), true}, sb, s));
+  OzGemm g{};
+  g.M = M; g.N = N; g.K = K; g.batch = 1; g.S = nslices;
+  g.C = C; g.c_sb = 0; g.c_r = lin(N); g.c_c = lin(1);
+  g.sym = SYM_NONE; g.tag = "ozaki_tc:dgemm";
+  return ozaki_gemm(sa, sb, g, s);
+}

@@ -151,3 +151,56 @@ def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
     _lib.call("gb_lagrange2_ri_f64", _ptr(C), _ptr(H), _ptr(b), _ptr(n), _ptr(cj12), _ptr(ck12), N, nbf5, Q,
               nbeta, nalpha, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
     return elag, Hmat
+
+
+# ----------------------------------------------------------------------------
+# split-product tensor-core path
+# ----------------------------------------------------------------------------
+def check_device_status() -> None:
+    """Raise if a tensor-core kernel recorded a timeout (synchronises)."""
+    st = _lib.device_status(reset=True)
+    if st != 0:
+        raise _lib.GBError(st, "a tensor-core kernel gave up on a bounded wait")
+
+
+def dgemm_mixed(A: torch.Tensor, B: torch.Tensor, nslices: int = 6) -> torch.Tensor:
+    """C = A B^T (FP64-accurate at nslices=6) on the tcgen05 tensor cores."""
+    M, K = A.shape
+    N, K2 = B.shape
+    if K2 != K:
+        raise ValueError("A and B must share K")
+    _require(A, (M, K), "A")
+    _require(B, (N, K), "B")
+    C = torch.empty((M, N), dtype=_F64, device=A.device)
+    wp, wn = _ws("gb_dgemm_mixed_workspace", M, N, K, nslices, device=A.device)
+    _lib.call("gb_dgemm_mixed", _ptr(A), _ptr(B), M, N, K, nslices, _ptr(C), wp, wn, _stream(A.device))
+    return C
+
+
+class PreparedRI:
+    """RI factor sliced for the tensor-core path (resident next to b)."""
+
+    def __init__(self, b: torch.Tensor, nslices: int = 6):
+        N, _, Q = b.shape
+        _require(b, (N, N, Q), "b")
+        self.nbf, self.naux, self.nslices = N, Q, nslices
+        nbytes = _lib.query("gb_ri_prepare_bytes_mixed", N, Q, nslices)
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=b.device)
+        _lib.call("gb_ri_prepare_mixed", _ptr(b), N, Q, nslices, self.buf.data_ptr(), nbytes, _stream(b.device))
+
+    @property
+    def device(self):
+        return self.buf.device
+
+
+def jkj_ri_mixed(C: torch.Tensor, prep: PreparedRI, nbf5: int):
+    """J, K (nbf5, nbf, nbf) on the tensor cores (A1, computeJKj)."""
+    N, Q, S = prep.nbf, prep.naux, prep.nslices
+    _require(C, (N, N), "C")
+    dev = prep.device
+    J = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    K = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_jkj_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
+    _lib.call("gb_jkj_ri_mixed", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J), _ptr(K), wp, wn,
+              _stream(dev))
+    return J, K

@@ -1,0 +1,83 @@
+"""Split-product tensor-core path (tcgen05) against FP64.
+
+Tolerances (normwise max|d| / max|ref|): nslices=6 must meet the FP64 bar of
+1e-10 (it lands near 1e-12); nslices=2 (bf16x3) is held to 1e-4.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, nrel, param_for
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_dgemm_small_integers_exact(torch_cuda):
+    """Integers below 128 are one exact digit: nslices=1 must be exact."""
+    from pynof_gb300 import ops
+
+    rng = np.random.default_rng(1)
+    A = rng.integers(-100, 100, (128, 32)).astype(np.float64)
+    B = rng.integers(-100, 100, (128, 32)).astype(np.float64)
+    C = ops.dgemm_mixed(ops.to_device(A), ops.to_device(B), nslices=1).cpu().numpy()
+    ops.check_device_status()
+    assert np.array_equal(C, A @ B.T)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 300, 500), (77, 130, 1000), (256, 384, 2400)])
+def test_dgemm_random(torch_cuda, M, N, K):
+    from pynof_gb300 import ops
+
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)) * np.exp(-0.05 * np.arange(M))[:, None]
+    B = rng.standard_normal((N, K))
+    ref = A @ B.T
+    for S, tol in ((6, 1e-10), (2, 1e-4)):
+        C = ops.dgemm_mixed(ops.to_device(A), ops.to_device(B), nslices=S).cpu().numpy()
+        ops.check_device_status()
+        err = nrel(C, ref)
+        assert err < tol, (S, err)
+
+
+@pytest.fixture(params=sorted(GOLDEN_CASES))
+def case(request, torch_cuda):
+    from pynof_gb300 import ops
+
+    name = request.param
+    g = load_golden(name)
+    return g, param_for(GOLDEN_CASES[name]), {k: ops.to_device(g[k]) for k in ("b", "C")}
+
+
+def test_jkj_ri_mixed_golden(case):
+    from pynof_gb300 import ops
+
+    g, p, d = case
+    prep = ops.PreparedRI(d["b"], nslices=6)
+    J, K = ops.jkj_ri_mixed(d["C"], prep, p.nbf5)
+    ops.check_device_status()
+    assert nrel(J.cpu().numpy(), g["J_ri"]) < 1e-10
+    assert nrel(K.cpu().numpy(), g["K_ri"]) < 1e-10
+
+
+@pytest.mark.parametrize("N,Q,ndoc,ncwo,seed", [(67, 131, 6, 4, 12), (150, 600, 15, 4, 5)])
+def test_jkj_ri_mixed_vs_oracle(torch_cuda, N, Q, ndoc, ncwo, seed):
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import ops, synthetic
+
+    st = synthetic.Structure(nbf=N, nbfaux=Q, ndoc=ndoc, ncwo=ncwo)
+    b, C, H, n = synthetic.make_inputs(st, seed)
+    Jr, Kr = orc.jkj_ri(C, b, st.nbf5)
+    db, dC = ops.to_device(b), ops.to_device(C)
+    for S, tol in ((6, 1e-10), (2, 1e-4)):
+        prep = ops.PreparedRI(db, nslices=S)
+        J, K = ops.jkj_ri_mixed(dC, prep, st.nbf5)
+        ops.check_device_status()
+        assert nrel(J.cpu().numpy(), Jr) < tol, (S, nrel(J.cpu().numpy(), Jr))
+        assert nrel(K.cpu().numpy(), Kr) < tol, (S, nrel(K.cpu().numpy(), Kr))
