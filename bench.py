@@ -6,7 +6,13 @@ nbf=600, naux=2400, nbf5=300 (seeded synthetic inputs; b is 6.9 GB, larger
 than L2, so no flush is needed between steps).
 
 Legs of the default run (``--impl ours``):
-  value   builds/s with b, C resident in HBM (device-timed, CUDA events);
+  value   builds/s with b, C resident in HBM (device-timed, CUDA events), on
+          the split-product tensor-core path (6 bf16 digit slices, FP64-class
+          accuracy; ``--precision fp64`` times the DMMA path instead);
+  fp64    the plain FP64 DMMA path on the same inputs (builds/s) and the
+          errors of the headline path against it: J, K normwise and the
+          electronic energy assembled from J, K (the no1 > 0 route of
+          ENERGY1r, closed shell) in FP64;
   e2e     builds/s through the reference-facing drop-in call
           ``pynof_gb300.integrals.JKj_RI_GPU(C, b, p)``: host C in (pinned),
           host J, K out (pinned), copies inside the timed region;
@@ -42,12 +48,15 @@ METRIC = "RI-JK builds/s at nbf=600 (computeJKj, J_i and K_i for i < nbf5)"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-sample", type=int, default=0, help="orbitals in the CPU sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--nslices", type=int, default=6)
+    ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
     return ap.parse_args()
 
 
@@ -58,12 +67,36 @@ def flops_jkj(N, P, Q):
 
 
 KERNEL_FLOPS = {
-    # per launch, reference formulation (symmetry the kernels exploit is not discounted)
+    # FP64 flops per launch in the reference formulation (symmetry the kernels
+    # exploit is not discounted)
     "gemm_f64:half_transform": lambda N, P, Q: 2.0 * P * N * N * Q,
     "gemm_f64:J": lambda N, P, Q: 2.0 * P * N * N * Q,
     "gemm_f64:K": lambda N, P, Q: 2.0 * P * N * N * Q,
     "contract_diag": lambda N, P, Q: 2.0 * P * N * Q,
+    "ozaki_tc:half_transform": lambda N, P, Q: 2.0 * P * N * N * Q,
+    "ozaki_tc:J": lambda N, P, Q: 2.0 * P * N * N * Q,
+    "ozaki_tc:K": lambda N, P, Q: 2.0 * P * N * N * Q,
 }
+
+
+def n_products(S):
+    """bf16 slice products per FP64 product: pairs (s, t) with s + t <= S + 1."""
+    return S * (S + 1) // 2
+
+
+def energy_from_jk(torch, J, K, C, H, n, cj, ck):
+    """Closed-shell electronic energy from J_i, K_i (FP64, torch):
+    E = sum_i C_i^T F_i C_i + sum_i n_i H_ii with the generalized Fock
+    F_i = n_i H + n_i J_i + sum_j cj_ij J_j - sum_j ck_ij K_j (zero diagonals),
+    i.e. computeF_RC -> computeLagrange -> computeE_elec with no1 = 0."""
+    P = J.shape[0]
+    Cp = C[:, :P]
+    Hd = torch.einsum("mi,mi->i", Cp, H @ Cp)
+    Jd = torch.einsum("mi,jmi->ji", Cp, torch.matmul(J, Cp))
+    Kd = torch.einsum("mi,jmi->ji", Cp, torch.matmul(K, Cp))
+    cj = cj.clone().fill_diagonal_(0.0)
+    ck = ck.clone().fill_diagonal_(0.0)
+    return float(2.0 * (n * Hd).sum() + (n * torch.diagonal(Jd)).sum() + (cj * Jd.T).sum() - (ck * Kd.T).sum())
 
 
 class ClockSampler:
@@ -200,6 +233,7 @@ def run_ours(args):
     N, P, Q = st.nbf, st.nbf5, st.nbfaux
     db = ops.to_device(b)
     dC = ops.to_device(C)
+    ops.check_device_status()
     asym = ops.check_symmetric(db)
     assert asym == 0.0, asym
 
@@ -215,9 +249,30 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    mixed = args.precision == "mixed"
+    S = args.nslices
+    integrals.set_precision(args.precision, S)
+
+    def build():
+        if mixed:
+            return ops.jkj_ri_mixed(dC, prep, P)
+        return ops.jkj_ri(dC, db, P)
+
+    # ---- one-time preparation of the resident sliced factor --------------
+    prep = None
+    prep_s = 0.0
+    if mixed:
+        barrier()
+        t0 = time.perf_counter()
+        prep = integrals.prepared(db, S)
+        barrier()
+        prep_s = time.perf_counter() - t0
+
     # ---- device-resident leg --------------------------------------------
     for _ in range(args.warmup):
-        J, K = ops.jkj_ri(dC, db, P)
+        J, K = build()
+    if mixed:
+        ops.check_device_status()
     del J, K
     props = torch.cuda.get_device_properties(dev)
     gpu_id = str(getattr(props, "uuid", local))
@@ -231,11 +286,13 @@ def run_ours(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        J, K = ops.jkj_ri(dC, db, P)
+        J, K = build()
     e1.record(stream)
     barrier()
     prof = _lib.profile_stop()
     clk = clocks.stop()
+    if mixed:
+        ops.check_device_status()
     dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3)
     value = world * args.steps / dev_s
 
@@ -254,6 +311,37 @@ def run_ours(args):
     e2e_value = world * args.steps / e2e_s
     h2d = C.nbytes
     d2h = 2 * P * N * N * 8
+    del Jh, Kh
+
+    # ---- FP64 DMMA comparison leg and accuracy of the headline path ------
+    fp64 = None
+    if mixed and args.fp64_steps > 0:
+        J64, K64 = ops.jkj_ri(dC, db, P)
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.fp64_steps):
+            J64, K64 = ops.jkj_ri(dC, db, P)
+        f1.record(stream)
+        barrier()
+        fp64_s = max_over_ranks(f0.elapsed_time(f1) / 1e3)
+        dH = ops.to_device(H)
+        dn = ops.to_device(n)
+        cj = 2.0 * torch.outer(dn, dn)
+        ck = torch.outer(dn, dn)
+        E64 = energy_from_jk(torch, J64, K64, dC, dH, dn, cj, ck)
+        Emx = energy_from_jk(torch, J, K, dC, dH, dn, cj, ck)
+
+        def nrel(a, r):
+            return float((a - r).abs().max() / r.abs().max())
+
+        fp64 = {"value": world * args.fp64_steps / fp64_s, "unit": "builds/s", "steps": args.fp64_steps,
+                "ms_per_step": 1e3 * fp64_s / args.fp64_steps,
+                "speedup_of_headline": value / (world * args.fp64_steps / fp64_s),
+                "J_normwise_err": nrel(J, J64), "K_normwise_err": nrel(K, K64),
+                "E_fp64_hartree": E64, "E_abs_err_hartree": abs(Emx - E64),
+                "energy_note": "closed-shell E from J_i, K_i with cj=2nn^T, ck=nn^T (zero diagonals)"}
+        del J64, K64
 
     # ---- roofline of the dominant kernel ---------------------------------
     peaks, peak_src = measured_peaks()
@@ -261,26 +349,40 @@ def run_ours(args):
     name, (launches, total_ms) = top
     per_launch_s = total_ms / 1e3 / launches
     fl = KERNEL_FLOPS.get(name, lambda N, P, Q: float("nan"))(N, P, Q)
-    achieved = fl / per_launch_s / 1e12
-    fp64_peak = measure_dgemm_tflops(torch, dev)
-    roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": achieved / fp64_peak, "traffic": None,
-            "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 path; MEASURED_PEAKS has no FP64 figure)",
-            "flops_per_launch": fl, "ms_per_launch": 1e3 * per_launch_s,
-            "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 3)} for k, v in prof.items()}}
+    if name.startswith("ozaki_tc"):
+        tensor_fl = n_products(S) * fl
+        achieved = tensor_fl / per_launch_s / 1e12
+        peak = float(peaks["bf16_tflops"])
+        roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": f"bf16_tflops of {peak_src} MEASURED_PEAKS.json (burst; kernel timed alone)",
+                "achieved_definition": f"{n_products(S)} bf16 slice products x reference-formulation flops "
+                                       "of the launch / launch time",
+                "fp64_equivalent_tflops": fl / per_launch_s / 1e12}
+    else:
+        fp64_peak = measure_dgemm_tflops(torch, dev)
+        achieved = fl / per_launch_s / 1e12
+        roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe; no FP64 figure is "
+                               "in MEASURED_PEAKS.json)"}
+    roof.update({"flops_per_launch_fp64": fl, "ms_per_launch": 1e3 * per_launch_s,
+                 "kernels": {k: {"launches": v[0], "total_ms": round(v[1], 3)} for k, v in prof.items()}})
 
     line = {
         "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P} (computeJKj)", "precision": "fp64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16-split-f64" if mixed else "f64", "data": "synthetic",
+        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P} (computeJKj)",
+                   "precision": f"mixed nslices={S} ({n_products(S)} bf16 products)" if mixed else "fp64",
                    "l2": "inputs larger than L2 (b = %.1f GB)" % (b.nbytes / 1e9),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "prepare_s": round(prep_s, 4)},
         "e2e": {"value": e2e_value, "unit": "builds/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roof,
         "gpu_launches": sum(v[0] for v in prof.values()),
         "clocks": clk,
-        "achieved_tflops_algorithmic": flops_jkj(N, P, Q) / (dev_s / args.steps) / 1e12,
+        "fp64_path": fp64,
     }
     if rank == 0 and not args.no_cpu_baseline:
         sample = args.cpu_sample or max(2, P // 5)

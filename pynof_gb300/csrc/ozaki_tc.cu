@@ -16,6 +16,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <cstdio>
 #include <mutex>
 
 #include "ozaki_tc.cuh"
@@ -27,6 +28,9 @@ namespace {
 
 constexpr int BM = 128, BN = 128, BK = 32, STAGES = 2, CH = 6;
 constexpr int NUM_EPI_WARPS = 16, THREADS = 32 * (2 + NUM_EPI_WARPS);
+// 18 warps put 5 warps on two of the four SM sub-partitions, whose register
+// files hold 16K registers each: 5 * 32 * 96 <= 16384 caps the kernel at 96.
+constexpr int MAX_REGS = 96;
 constexpr uint32_t TILE_BYTES = BM * BK * 2;  // 8 KB per slice tile (BM == BN)
 constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
@@ -171,7 +175,7 @@ struct KArgs {
   int frac;
 };
 
-__global__ void __maxnreg__(112)
+__global__ void __maxnreg__(MAX_REGS)
     ozaki_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const KArgs a) {
   extern __shared__ unsigned char smem_raw[];
   const OzGemm& g = a.g;
@@ -491,7 +495,35 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   if (frac < 0) frac = 0;
   KArgs ka{g, A.exps, B.exps, frac};
   dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)g.batch);
-  GB_LAUNCH(g.tag, stream, ozaki_kernel<<<grid, THREADS, smem, stream>>>(ma, mb, ka));
+  const int pi = prof_begin(g.tag, stream);
+  ozaki_kernel<<<grid, THREADS, smem, stream>>>(ma, mb, ka);
+  prof_end(pi, stream);
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) {
+    char info[512];
+    ozaki_kernel_info(info, sizeof(info));
+    set_error(GB_ERR_CUDA, "%s: %s (threads %d, dynamic smem %zu; %s)", g.tag, cudaGetErrorString(le), THREADS,
+              smem, info);
+    return GB_ERR_CUDA;
+  }
+  return GB_OK;
+}
+
+int ozaki_kernel_info(char* out, size_t len) {
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, ozaki_kernel);
+  int occ = -1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ozaki_kernel, THREADS, smem_bytes(6));
+  int dev = 0, regs_sm = 0, smem_optin = 0, max_thr = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&max_thr, cudaDevAttrMaxThreadsPerBlock, dev);
+  snprintf(out, len,
+           "attr=%s regs=%d maxThreadsPerBlock=%d localBytes=%zu staticSmem=%zu maxDynSmem=%d occupancy=%d "
+           "regsPerSM=%d smemOptin=%d devMaxThreads=%d",
+           cudaGetErrorString(e), fa.numRegs, fa.maxThreadsPerBlock, fa.localSizeBytes, fa.sharedSizeBytes,
+           fa.maxDynamicSharedSizeBytes, occ, regs_sm, smem_optin, max_thr);
   return GB_OK;
 }
 

@@ -40,4 +40,7 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
 // bounded wait gave up).  Reading synchronises the current device.
 int ozaki_status(int reset, int* out);
 
+// Launch attributes of the kernel (registers, limits, occupancy) as text.
+int ozaki_kernel_info(char* out, size_t len);
+
 }  // namespace gb

@@ -16,10 +16,48 @@ All arithmetic runs in ``libpynof_gb300.so``; there is no CPU fallback.
 """
 from __future__ import annotations
 
+import threading
+import weakref
+
 import numpy as np
 import torch
 
 from . import ops
+
+#: Arithmetic of the device path: "fp64" (DMMA) or "mixed" (tcgen05 digit
+#: slices; nslices=6 agrees with FP64 to ~1e-11, nslices=2 is bf16x3).
+PRECISION = {"mode": "mixed", "nslices": 6}
+
+_prep_lock = threading.Lock()
+# id(b) -> (weakref to b, b._version, {nslices: PreparedRI}); entries die with b
+_prepared: dict = {}
+
+
+def set_precision(mode: str, nslices: int = 6) -> None:
+    if mode not in ("fp64", "mixed"):
+        raise ValueError(f"unknown precision mode {mode!r}")
+    if not 1 <= nslices <= 6:
+        raise ValueError("nslices must be in [1, 6]")
+    PRECISION["mode"] = mode
+    PRECISION["nslices"] = nslices
+
+
+def prepared(b: torch.Tensor, nslices: int) -> ops.PreparedRI:
+    """The sliced RI factor for ``b`` (built once per tensor and slice count)."""
+    key = id(b)
+    with _prep_lock:
+        ent = _prepared.get(key)
+        if ent is not None and (ent[0]() is not b or ent[1] != b._version):
+            ent = None
+        if ent is not None and nslices in ent[2]:
+            return ent[2][nslices]
+        prep = ops.PreparedRI(b, nslices)
+        if ent is None:
+            ref = weakref.ref(b, lambda _r, k=key: _prepared.pop(k, None))
+            ent = (ref, b._version, {})
+            _prepared[key] = ent
+        ent[2][nslices] = prep
+        return prep
 
 
 def as_device(x) -> torch.Tensor:
@@ -62,10 +100,17 @@ def upload_integrals(I, b_mnl, check_symmetry: bool = True):
 # ---------------------------------------------------------------------------
 # A1  computeJKj
 # ---------------------------------------------------------------------------
+def jkj_ri_device(C, b_mnl, nbf5):
+    """J, K as CUDA tensors with the arithmetic selected by ``PRECISION``."""
+    dC, db = as_device(C), as_device(b_mnl)
+    if PRECISION["mode"] == "mixed":
+        return ops.jkj_ri_mixed(dC, prepared(db, PRECISION["nslices"]), nbf5)
+    return ops.jkj_ri(dC, db, nbf5)
+
+
 def JKj_RI_GPU(C, b_mnl, p):
     """J, K (nbf5, nbf, nbf) -- ``pynof/integrals.py:234-245``."""
-    J, K = ops.jkj_ri(as_device(C), as_device(b_mnl), p.nbf5)
-    return to_host(J, K)
+    return to_host(*jkj_ri_device(C, b_mnl, p.nbf5))
 
 
 def computeJKj(C, I, b_mnl, p):
