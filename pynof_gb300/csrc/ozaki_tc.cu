@@ -1,19 +1,20 @@
 // tcgen05 split-product FP64 GEMM (see ozaki_tc.cuh).
 //
-// CTA: 18 warps.  warp 0 lane 0 issues TMA loads (2-stage ring, every stage
-// holds the S slices of a 128 x 32 A tile and of a 128 x 32 B tile, 64-byte
-// swizzled, K-major); warp 1 allocates TMEM (512 columns) and its lane 0
-// issues tcgen05.mma (M=128, N=128, K=16, bf16 -> f32); warps 2..17 drain and
-// finish: warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows) and columns
-// 32 ((w - 2) / 4) .. +31 of every accumulator.
+// CTA: 18 warps.  warp 0 lane 0 is the producer: a 4-stage ring in which every
+// stage holds the S slices of a 128 x 16 block of A and of B, each operand one
+// contiguous cp.async.bulk copy (the slicer stores the digits in the
+// tensor-core core-matrix order, slice.cuh).  warp 1 allocates TMEM (512
+// columns) and its lane 0 issues tcgen05.mma (M=128, N=128, K=16,
+// bf16 -> f32).  warps 2..17 drain and finish: warp w reads TMEM lanes
+// 32 (w % 4) .. +31 (tile rows) and columns 32 ((w - 2) / 4) .. +31 of every
+// accumulator.
 //
 // TMEM columns: [0,128) group 2, [128,256) group 3, [256,384) group 4 (exact,
-// drained every 6 stages = 192 k), [384,512) groups 5.. (whole K).
+// drained every 12 stages = 192 k), [384,512) groups 5.. (whole K).
 //
 // Every mbarrier wait is bounded (kWaitLimitNs); on timeout the CTA records
 // GB_ERR_TIMEOUT in the device status word, stops issuing work, waits (bounded)
 // for its own TMA copies and MMAs in flight, frees TMEM and exits.
-#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cstdio>
@@ -26,12 +27,12 @@ static __device__ int g_tc_status;
 namespace gb {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 32, STAGES = 2, CH = 6;
+constexpr int BM = 128, BN = 128, BK = SL_K, STAGES = 4, CH = 12;
 constexpr int NUM_EPI_WARPS = 16, THREADS = 32 * (2 + NUM_EPI_WARPS);
 // 18 warps put 5 warps on two of the four SM sub-partitions, whose register
 // files hold 16K registers each: 5 * 32 * 96 <= 16384 caps the kernel at 96.
 constexpr int MAX_REGS = 96;
-constexpr uint32_t TILE_BYTES = BM * BK * 2;  // 8 KB per slice tile (BM == BN)
+constexpr uint32_t TILE_BYTES = SL_TILE_BYTES;  // 4 KB per slice tile (BM == BN == SL_ROWS)
 constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
 constexpr float MAGIC = 12582912.0f;                          // 1.5 * 2^23
@@ -86,23 +87,22 @@ __device__ __forceinline__ void signal_abort(volatile int* abort_flag) {
   atomicExch(&g_tc_status, GB_ERR_TIMEOUT);
 }
 
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-      : "memory");
+// Contiguous global -> shared bulk copy completing on an mbarrier.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
 }
 
-// UMMA shared-memory descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart.
-__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+// UMMA shared-memory descriptor of one 128 x 16 slice tile: K-major, no
+// swizzle; core matrices (8 rows x 16 B) 2 KB apart along K (leading byte
+// offset) and 128 B apart along the rows (stride byte offset).
+__device__ __forceinline__ uint64_t desc_tile(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512u >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)(2048u >> 4) << 16;   // leading byte offset
+  d |= (uint64_t)(128u >> 4) << 32;    // stride byte offset
   d |= (uint64_t)1 << 46;              // descriptor version
-  d |= (uint64_t)4 << 61;              // SWIZZLE_64B
-  return d;
+  return d;                            // layout type 0: no swizzle
 }
 
 // kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major, M=128, N=128.
@@ -125,13 +125,11 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-      : "r"(taddr)
-      : "memory");
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr)
+               : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
@@ -170,18 +168,51 @@ __device__ __forceinline__ double fixed_to_double(long long z, int scale, int ne
 
 struct KArgs {
   OzGemm g;
-  const int* expA;
-  const int* expB;
+  SlicedDesc A, B;
   int frac;
 };
 
-__global__ void __maxnreg__(MAX_REGS)
-    ozaki_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const KArgs a) {
+// MMAs of one stage, fully unrolled for S slices: a product (s, t) reads slice
+// tile s of A and t of B, whose descriptors differ from the stage's first tile
+// descriptors only in the start-address field (+ (s - 1) * TILE_BYTES / 16).
+template <int S>
+__device__ __forceinline__ void issue_inexact(uint32_t tmem, uint64_t da, uint64_t db, bool& started) {
+#pragma unroll
+  for (int s = 1; s <= S; ++s)
+#pragma unroll
+    for (int t = 1; t <= S + 1 - s; ++t) {
+      if (s + t <= 4) continue;
+      mma_bf16(tmem + 384, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)), db + (uint64_t)((t - 1) * (TILE_BYTES >> 4)),
+               started);
+      started = true;
+    }
+}
+
+template <int S>
+__device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t db, bool first) {
+  constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
+#pragma unroll
+  for (int gg = 2; gg <= gE; ++gg) {
+#pragma unroll
+    for (int s = 1; s < gg; ++s) {
+      const int t = gg - s;
+      if (s > S || t > S) continue;
+      mma_bf16(tmem + (gg - 2) * 128, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)),
+               db + (uint64_t)((t - 1) * (TILE_BYTES >> 4)), !(first && s == 1));
+    }
+  }
+}
+
+template <int SLICES>
+__global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs a) {
   extern __shared__ unsigned char smem_raw[];
   const OzGemm& g = a.g;
-  const int m0 = blockIdx.y * BM;
-  const int n0 = blockIdx.x * BN;
-  const int bz = blockIdx.z;
+  // M tiles vary fastest, so the CTAs that share a B tile run together and the
+  // B slices are read from HBM once (L2 serves the other M tiles).
+  const int mtiles = (g.M + BM - 1) / BM;
+  const int m0 = (int)(blockIdx.x % mtiles) * BM;
+  const int n0 = (int)(blockIdx.x / mtiles) * BN;
+  const int bz = blockIdx.y;
 
   if (g.sym == SYM_ROWCOL && m0 > n0) return;
   if (g.sym == SYM_PAIRCOL) {
@@ -192,18 +223,19 @@ __global__ void __maxnreg__(MAX_REGS)
   // a CTA of this or an earlier launch gave up: do not start (the host sees the status word)
   if (*(volatile int*)&g_tc_status != 0) return;
 
-  const int S = g.S;
+  constexpr int S = SLICES;
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t stage_bytes = 2u * S * TILE_BYTES;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
-  // bars: full[0..1], empty[0..1], accfull, accempty, done
-  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 8);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 9);
+  // bars: full[STAGES], empty[STAGES], accfull, accempty, done
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
   const uint32_t sbase = smem_u32(smem);
   const uint32_t bar0 = smem_u32(bars);
   auto full_bar = [&](int st) { return bar0 + 8u * st; };
-  auto empty_bar = [&](int st) { return bar0 + 8u * (2 + st); };
-  const uint32_t accfull_bar = bar0 + 8u * 4, accempty_bar = bar0 + 8u * 5, done_bar = bar0 + 8u * 6;
+  auto empty_bar = [&](int st) { return bar0 + 8u * (STAGES + st); };
+  const uint32_t accfull_bar = bar0 + 8u * (2 * STAGES), accempty_bar = bar0 + 8u * (2 * STAGES + 1),
+                 done_bar = bar0 + 8u * (2 * STAGES + 2);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -219,10 +251,6 @@ __global__ void __maxnreg__(MAX_REGS)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  if (warp == 0 && lane == 0) {
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
-    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -245,23 +273,28 @@ __global__ void __maxnreg__(MAX_REGS)
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       int issued = 0;
+      const uint32_t half = (uint32_t)S * TILE_BYTES;
+      const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + (long long)bz * a.A.batch_bytes() +
+                                (long long)(m0 / BM) * a.A.kblocks() * half;
+      const unsigned char* gb_ = reinterpret_cast<const unsigned char*>(a.B.planes) + (long long)bz * a.B.batch_bytes() +
+                                 (long long)(n0 / BN) * a.B.kblocks() * half;
       for (int kb = 0; kb < nkb; ++kb) {
-        const int st = kb & 1;
-        const uint32_t ph = (kb >> 1) & 1;
+        const int st = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
         if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag)) {
           signal_abort(abort_flag);
           break;
         }
         mbar_expect_tx(full_bar(st), stage_bytes);
         const uint32_t sa = sbase + st * stage_bytes;
-        for (int s = 0; s < S; ++s) tma_load_3d(sa + s * TILE_BYTES, &tmA, kb * BK, m0, bz * S + s, full_bar(st));
-        for (int s = 0; s < S; ++s)
-          tma_load_3d(sa + (S + s) * TILE_BYTES, &tmB, kb * BK, n0, bz * S + s, full_bar(st));
+        bulk_load(sa, ga + (long long)kb * half, half, full_bar(st));
+        bulk_load(sa + half, gb_ + (long long)kb * half, half, full_bar(st));
         ++issued;
       }
       if (*abort_flag) {
         // let the copies this thread issued land before the CTA exits
-        for (int kb = max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full_bar(kb & 1), (kb >> 1) & 1, nullptr);
+        for (int kb = max(0, issued - STAGES); kb < issued; ++kb)
+          mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1, nullptr);
       }
     }
   } else if (warp == 1) {
@@ -269,25 +302,15 @@ __global__ void __maxnreg__(MAX_REGS)
     if (lane == 0) {
       bool f_started = false;
       for (int kb = 0; kb < nkb; ++kb) {
-        const int st = kb & 1;
-        if (!mbar_wait(full_bar(st), (kb >> 1) & 1, abort_flag)) {
+        const int st = kb % STAGES;
+        if (!mbar_wait(full_bar(st), (kb / STAGES) & 1, abort_flag)) {
           signal_abort(abort_flag);
           break;
         }
         tc_fence_after();
         const uint32_t sa = sbase + st * stage_bytes;
-        const uint32_t sb = sa + S * TILE_BYTES;
-        if (has_inexact) {
-          for (int s = 1; s <= S; ++s)
-            for (int t = 1; t <= S + 1 - s; ++t) {
-              if (s + t <= 4) continue;
-              for (int ks = 0; ks < BK / 16; ++ks) {
-                mma_bf16(tmem + 384, desc_sw64(sa + (s - 1) * TILE_BYTES + ks * 32),
-                         desc_sw64(sb + (t - 1) * TILE_BYTES + ks * 32), f_started);
-                f_started = true;
-              }
-            }
-        }
+        const uint64_t da = desc_tile(sa), db = desc_tile(sa + S * TILE_BYTES);
+        if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
         const int c = kb / CH;
         const bool first = (kb % CH) == 0;
         if (first && c > 0) {
@@ -297,18 +320,7 @@ __global__ void __maxnreg__(MAX_REGS)
           }
           tc_fence_after();
         }
-        for (int gg = 2; gg <= gE; ++gg) {
-          bool acc = !first;
-          for (int s = 1; s < gg; ++s) {
-            const int t = gg - s;
-            if (s > S || t > S) continue;
-            for (int ks = 0; ks < BK / 16; ++ks) {
-              mma_bf16(tmem + (gg - 2) * 128, desc_sw64(sa + (s - 1) * TILE_BYTES + ks * 32),
-                       desc_sw64(sb + (t - 1) * TILE_BYTES + ks * 32), acc);
-              acc = true;
-            }
-          }
-        }
+        issue_exact<S>(tmem, da, db, first);
         if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(accfull_bar);
         mma_commit(empty_bar(st));
       }
@@ -335,14 +347,14 @@ __global__ void __maxnreg__(MAX_REGS)
         const float up = __int_as_float((127 + 7 * gg) << 23);  // 2^(7 g)
         const int sh = 7 * (gE - gg);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint32_t v[16];
-          tmem_ld16(lbase + (uint32_t)((gg - 2) * 128 + h * 16), v);
+        for (int h = 0; h < 4; ++h) {
+          uint32_t v[8];
+          tmem_ld8(lbase + (uint32_t)((gg - 2) * 128 + h * 8), v);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 8; ++j) {
             const float f = fmaf(__uint_as_float(v[j]), up, MAGIC);
             const long long iv = (long long)(__float_as_int(f) - MAGIC_BITS);
-            R[h * 16 + j] += (long long)((unsigned long long)iv << sh);
+            R[h * 8 + j] += (long long)((unsigned long long)iv << sh);
           }
         }
       }
@@ -362,29 +374,29 @@ __global__ void __maxnreg__(MAX_REGS)
       const int i = m0 + q * 32 + lane;
       const float upE = __int_as_float((127 + 7 * gE) << 23);
       const float upF = __int_as_float((127 + a.frac) << 23);
-      const int ea = (i < g.M) ? a.expA[(long long)bz * g.M + i] : 0;
+      const int ea = (i < g.M) ? a.A.exps[(long long)bz * g.M + i] : 0;
       double* Cb = g.C + (long long)bz * g.c_sb;
       const long long ri = (i < g.M) ? g.c_r.at(i) : 0;
       const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        uint32_t v[16];
+      for (int h = 0; h < 4; ++h) {
+        uint32_t v[8];
         if (has_inexact) {
-          tmem_ld16(lbase + 384u + (uint32_t)(h * 16), v);
+          tmem_ld8(lbase + 384u + (uint32_t)(h * 8), v);
         } else {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = 0u;
+          for (int j = 0; j < 8; ++j) v[j] = 0u;
         }
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int jj = n0 + cg * 32 + h * 16 + j;
+        for (int j = 0; j < 8; ++j) {
+          const int jj = n0 + cg * 32 + h * 8 + j;
           if (i >= g.M || jj >= g.N) continue;
           const float t = __uint_as_float(v[j]) * upE;
           const float th = rintf(t);
           const long long hi = __float2ll_rn(th);
           const long long lo = __float2ll_rn((t - th) * upF);
-          const long long z = (long long)((unsigned long long)(R[h * 16 + j] + hi) << a.frac) + lo;
-          const int eb = a.expB[(long long)bz * g.N + jj];
+          const long long z = (long long)((unsigned long long)(R[h * 8 + j] + hi) << a.frac) + lo;
+          const int eb = a.B.exps[(long long)bz * g.N + jj];
           const double val = fixed_to_double(z, ea + eb - 7 * gE - a.frac, g.negate);
           Cb[ri + g.c_c.at(jj)] = val;
           if (mirror_rc) {
@@ -412,43 +424,19 @@ __global__ void __maxnreg__(MAX_REGS)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-int get_encode(EncodeFn* out) {
-  static std::mutex mu;
-  static EncodeFn fn = nullptr;
-  std::lock_guard<std::mutex> lk(mu);
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
-    GB_REQUIRE(e == cudaSuccess && q == cudaDriverEntryPointSuccess && p, GB_ERR_CUDA,
-               "cuTensorMapEncodeTiled unavailable (%s)", cudaGetErrorString(e));
-    fn = reinterpret_cast<EncodeFn>(p);
-  }
-  *out = fn;
-  return GB_OK;
-}
-
-int make_map(const SlicedDesc& d, CUtensorMap* map) {
-  EncodeFn enc;
-  GB_TRY(get_encode(&enc));
-  GB_REQUIRE((reinterpret_cast<uintptr_t>(d.planes) & 15) == 0, GB_ERR_INVALID_ARG, "slice planes not 16-byte aligned");
-  cuuint64_t dims[3] = {(cuuint64_t)d.K, (cuuint64_t)d.rows, (cuuint64_t)d.batch * d.S};
-  cuuint64_t strides[2] = {(cuuint64_t)d.kpad * 2, (cuuint64_t)d.rows * d.kpad * 2};
-  cuuint32_t box[3] = {BK, BM, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, d.planes, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  GB_REQUIRE(r == CUDA_SUCCESS, GB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) dims %llu x %llu x %llu", (int)r,
-             (unsigned long long)dims[0], (unsigned long long)dims[1], (unsigned long long)dims[2]);
-  return GB_OK;
-}
-
 size_t smem_bytes(int S) { return (size_t)STAGES * 2 * S * TILE_BYTES + 256 + 1024; }
+
+using KernelFn = void (*)(KArgs);
+KernelFn kernel_for(int S) {
+  switch (S) {
+    case 1: return ozaki_kernel<1>;
+    case 2: return ozaki_kernel<2>;
+    case 3: return ozaki_kernel<3>;
+    case 4: return ozaki_kernel<4>;
+    case 5: return ozaki_kernel<5>;
+    default: return ozaki_kernel<6>;
+  }
+}
 
 }  // namespace
 
@@ -461,14 +449,13 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   GB_REQUIRE(g.sym != SYM_ROWCOL || g.M == g.N, GB_ERR_BAD_SHAPE, "ozaki_gemm: SYM_ROWCOL needs M == N");
   GB_REQUIRE(g.sym != SYM_PAIRCOL || (long long)g.pair_n * g.pair_n == g.N, GB_ERR_BAD_SHAPE,
              "ozaki_gemm: SYM_PAIRCOL needs N == pair_n^2");
-  const long long gy = (g.M + BM - 1) / BM, gx = (g.N + BN - 1) / BN;
-  GB_REQUIRE(gy <= 65535 && g.batch <= 65535 && gx <= 2147483647LL, GB_ERR_BAD_SHAPE, "ozaki_gemm: grid too large");
+  const long long tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
+  GB_REQUIRE(g.batch <= 65535 && tiles <= 2147483647LL, GB_ERR_BAD_SHAPE, "ozaki_gemm: grid too large");
   if (g.K == 0) {
     GB_REQUIRE(false, GB_ERR_BAD_SHAPE, "ozaki_gemm: K == 0");
   }
-  CUtensorMap ma, mb;
-  GB_TRY(make_map(A, &ma));
-  GB_TRY(make_map(B, &mb));
+  GB_REQUIRE((reinterpret_cast<uintptr_t>(A.planes) & 15) == 0 && (reinterpret_cast<uintptr_t>(B.planes) & 15) == 0,
+             GB_ERR_INVALID_ARG, "ozaki_gemm: slice planes not 16-byte aligned");
   const size_t smem = smem_bytes(g.S);
   static std::mutex mu;
   static int configured_dev[64] = {0};
@@ -477,9 +464,10 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
     GB_TRY(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
     std::lock_guard<std::mutex> lk(mu);
     if (dev >= 0 && dev < 64 && !configured_dev[dev]) {
-      GB_TRY(cuda_status(cudaFuncSetAttribute(ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem_bytes(6)),
-                         "cudaFuncSetAttribute"));
+      for (int sl = 1; sl <= 6; ++sl)
+        GB_TRY(cuda_status(cudaFuncSetAttribute(kernel_for(sl), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_bytes(sl)),
+                           "cudaFuncSetAttribute"));
       configured_dev[dev] = 1;
     }
   }
@@ -493,10 +481,10 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   int frac = 62 - rbits;
   if (frac > 16) frac = 16;
   if (frac < 0) frac = 0;
-  KArgs ka{g, A.exps, B.exps, frac};
-  dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)g.batch);
+  KArgs ka{g, A, B, frac};
+  dim3 grid((unsigned)tiles, (unsigned)g.batch);
   const int pi = prof_begin(g.tag, stream);
-  ozaki_kernel<<<grid, THREADS, smem, stream>>>(ma, mb, ka);
+  kernel_for(g.S)<<<grid, THREADS, smem, stream>>>(ka);
   prof_end(pi, stream);
   const cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) {
@@ -511,9 +499,9 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
 
 int ozaki_kernel_info(char* out, size_t len) {
   cudaFuncAttributes fa{};
-  cudaError_t e = cudaFuncGetAttributes(&fa, ozaki_kernel);
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel_for(6));
   int occ = -1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ozaki_kernel, THREADS, smem_bytes(6));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(6), THREADS, smem_bytes(6));
   int dev = 0, regs_sm = 0, smem_optin = 0, max_thr = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);

@@ -19,14 +19,11 @@ struct Prepared {
 
 template <class C>
 void prepared_layout(C& c, int N, int Q, int S, Prepared* out) {
-  const int kN = slice_kpad(N), kQ = slice_kpad(Q);
-  auto* tp = c.template take<__nv_bfloat16>((size_t)S * N * Q * kN);
-  auto* te = c.template take<int>((size_t)N * Q);
-  auto* jp = c.template take<__nv_bfloat16>((size_t)S * N * N * kQ);
-  auto* je = c.template take<int>((size_t)N * N);
+  SlicedDesc t = take_sliced(c, 1, N * Q, N, S);
+  SlicedDesc j = take_sliced(c, 1, N * N, Q, S);
   if (out) {
-    out->bT = SlicedDesc{tp, te, 1, N * Q, N, kN, S};
-    out->bJ = SlicedDesc{jp, je, 1, N * N, Q, kQ, S};
+    out->bT = t;
+    out->bJ = j;
   }
 }
 
@@ -56,21 +53,17 @@ struct JkjMixedWs {
 
 template <class C>
 void jkj_mixed_layout(C& c, int N, int P, int Q, int S, JkjMixedWs* w) {
-  const int kN = slice_kpad(N), kQ = slice_kpad(Q);
-  auto* ap = c.template take<__nv_bfloat16>((size_t)S * P * kN);
-  auto* ae = c.template take<int>((size_t)P);
+  SlicedDesc A = take_sliced(c, 1, P, N, S);
   auto* tf = c.template take<double>((size_t)P * N * Q);
   auto* dv = c.template take<double>((size_t)P * Q);
-  auto* dp = c.template take<__nv_bfloat16>((size_t)S * P * kQ);
-  auto* de = c.template take<int>((size_t)P);
-  auto* tp = c.template take<__nv_bfloat16>((size_t)P * S * N * kQ);
-  auto* te = c.template take<int>((size_t)P * N);
+  SlicedDesc d = take_sliced(c, 1, P, Q, S);
+  SlicedDesc T = take_sliced(c, P, N, Q, S);
   if (w) {
-    w->A = SlicedDesc{ap, ae, 1, P, N, kN, S};
+    w->A = A;
     w->Tf = tf;
     w->dv = dv;
-    w->d = SlicedDesc{dp, de, 1, P, Q, kQ, S};
-    w->T = SlicedDesc{tp, te, P, N, Q, kQ, S};
+    w->d = d;
+    w->T = T;
   }
 }
 
@@ -163,13 +156,10 @@ extern "C" int gb_device_status(int reset, int* status) {
 namespace {
 template <class Cv>
 void dgemm_layout(Cv& c, int M, int N, int K, int S, SlicedDesc* a, SlicedDesc* b) {
-  const int kp = slice_kpad(K);
-  auto* ap = c.template take<__nv_bfloat16>((size_t)S * M * kp);
-  auto* ae = c.template take<int>((size_t)M);
-  auto* bp = c.template take<__nv_bfloat16>((size_t)S * N * kp);
-  auto* be = c.template take<int>((size_t)N);
-  if (a) *a = SlicedDesc{ap, ae, 1, M, K, kp, S};
-  if (b) *b = SlicedDesc{bp, be, 1, N, K, kp, S};
+  SlicedDesc sa = take_sliced(c, 1, M, K, S);
+  SlicedDesc sb = take_sliced(c, 1, N, K, S);
+  if (a) *a = sa;
+  if (b) *b = sb;
 }
 }  // namespace
 

@@ -4,8 +4,6 @@
 namespace gb {
 namespace {
 
-constexpr int TILE = 32;
-
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
@@ -75,52 +73,41 @@ __global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restri
   exps[b * rows + row] = exponent_of(mx);
 }
 
-// 32 x 32 tiles, 32 x 8 threads.  KFAST: load and store along k directly.
-// Otherwise load along rows, transpose through shared memory, store along k.
-template <bool KFAST>
-__global__ void digits_kernel(SliceSrc src, SlicedDesc dst, int tiles_k) {
-  __shared__ __nv_bfloat16 sm[KFAST ? 1 : 6][TILE][TILE + 2];
+// One CTA of 256 threads per (row block, k block): thread -> (row r, k group of
+// 8).  Lanes 0..7 take consecutive rows of one core matrix and a warp covers
+// 32 consecutive rows of one k group, i.e. four whole consecutive core
+// matrices (512 contiguous bytes) per slice, written with 16-byte stores; it
+// reads 64 contiguous source bytes per row (K-fast sources) or 256 contiguous
+// bytes per k (row-fast sources).
+__global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, SlicedDesc dst) {
   const long long b = blockIdx.y;
-  const int tr = blockIdx.x / tiles_k, tk = blockIdx.x % tiles_k;
-  const int r0 = tr * TILE, k0 = tk * TILE;
+  const int kbn = dst.kblocks();
+  const int rb = blockIdx.x / kbn, kb = blockIdx.x % kbn;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ri = lane & 7, kg = warp >> 2, rg = (warp & 3) * 4 + (lane >> 3);
+  const int r = rb * SL_ROWS + rg * 8 + ri;
+  const int k0 = kb * SL_K + kg * 8;
   const int S = dst.S;
-  const double* base = src.p + b * src.sb;
-  const int* ex = dst.exps + b * dst.rows;
-  __nv_bfloat16* planes = dst.planes + b * (long long)S * dst.rows * dst.kpad;
-  const long long plane_stride = (long long)dst.rows * dst.kpad;
-  __nv_bfloat16 dg[6];
-  if (KFAST) {
-    const int k = k0 + threadIdx.x;
-    for (int i = threadIdx.y; i < TILE; i += blockDim.y) {
-      const int r = r0 + i;
-      if (r >= dst.rows || k >= dst.kpad) continue;
-      double x = 0.0;
-      if (k < dst.K) x = base[src.r.at(r) + src.k.at(k)];
-      make_digits(x, ex[r], S, dg);
-      __nv_bfloat16* o = planes + (long long)r * dst.kpad + k;
-      for (int s = 0; s < S; ++s) o[s * plane_stride] = dg[s];
-    }
-  } else {
-    const int r = r0 + threadIdx.x;
-    for (int i = threadIdx.y; i < TILE; i += blockDim.y) {
-      const int k = k0 + i;
-      double x = 0.0;
-      int e = 0;
-      if (r < dst.rows) {
-        e = ex[r];
-        if (k < dst.K) x = base[src.r.at(r) + src.k.at(k)];
-      }
-      make_digits(x, e, S, dg);
-      for (int s = 0; s < S; ++s) sm[s][i][threadIdx.x] = dg[s];
-    }
-    __syncthreads();
-    const int k = k0 + threadIdx.x;
-    for (int i = threadIdx.y; i < TILE; i += blockDim.y) {
-      const int rr = r0 + i;
-      if (rr >= dst.rows || k >= dst.kpad) continue;
-      __nv_bfloat16* o = planes + (long long)rr * dst.kpad + k;
-      for (int s = 0; s < S; ++s) o[s * plane_stride] = sm[s][threadIdx.x][i];
-    }
+  __nv_bfloat16 dg[8][6];
+  const bool rok = r < dst.rows;
+  const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
+  const int e = rok ? dst.exps[b * dst.rows + r] : 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = k0 + u;
+    const double x = (rok && k < dst.K) ? base[src.k.at(k)] : 0.0;
+    make_digits(x, e, S, dg[u]);
+  }
+  unsigned char* out = reinterpret_cast<unsigned char*>(dst.planes) + b * dst.batch_bytes() +
+                       ((long long)blockIdx.x * S) * SL_TILE_BYTES + (kg * 16 + rg) * 128 + ri * 16;
+  for (int s = 0; s < S; ++s) {
+    uint4 v;
+    __nv_bfloat162 t;
+    t.x = dg[0][s]; t.y = dg[1][s]; v.x = *reinterpret_cast<unsigned*>(&t);
+    t.x = dg[2][s]; t.y = dg[3][s]; v.y = *reinterpret_cast<unsigned*>(&t);
+    t.x = dg[4][s]; t.y = dg[5][s]; v.z = *reinterpret_cast<unsigned*>(&t);
+    t.x = dg[6][s]; t.y = dg[7][s]; v.w = *reinterpret_cast<unsigned*>(&t);
+    *reinterpret_cast<uint4*>(out + (long long)s * SL_TILE_BYTES) = v;
   }
 }
 
@@ -130,8 +117,9 @@ inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) /
 
 int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
   GB_REQUIRE(dst.S >= 1 && dst.S <= 6, GB_ERR_INVALID_ARG, "slice_operand: nslices=%d outside [1, 6]", dst.S);
-  GB_REQUIRE(dst.kpad == slice_kpad(dst.K), GB_ERR_INVALID_ARG, "slice_operand: kpad mismatch");
   GB_REQUIRE(dst.batch >= 1 && dst.batch <= 65535 && dst.rows >= 0, GB_ERR_BAD_SHAPE, "slice_operand: bad batch");
+  GB_REQUIRE((reinterpret_cast<uintptr_t>(dst.planes) & 15) == 0, GB_ERR_INVALID_ARG,
+             "slice_operand: planes not 16-byte aligned");
   if (dst.rows == 0 || dst.K == 0) return GB_OK;
   if (src.kfast) {
     GB_LAUNCH("slice_rowexp", s,
@@ -140,16 +128,9 @@ int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
     GB_LAUNCH("slice_rowexp", s,
               rowexp_rfast_kernel<<<dim3(cdiv(dst.rows, 256), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K, dst.exps));
   }
-  const long long tiles_k = cdiv(dst.kpad, TILE);
-  const long long tiles = cdiv(dst.rows, TILE) * tiles_k;
-  GB_REQUIRE(tiles <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many tiles");
-  if (src.kfast) {
-    GB_LAUNCH("slice_digits", s,
-              digits_kernel<true><<<dim3((unsigned)tiles, dst.batch), dim3(TILE, 8), 0, s>>>(src, dst, (int)tiles_k));
-  } else {
-    GB_LAUNCH("slice_digits", s,
-              digits_kernel<false><<<dim3((unsigned)tiles, dst.batch), dim3(TILE, 8), 0, s>>>(src, dst, (int)tiles_k));
-  }
+  const long long blocks = (long long)dst.rblocks() * dst.kblocks();
+  GB_REQUIRE(blocks <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many blocks");
+  GB_LAUNCH("slice_digits", s, digits_blocked_kernel<<<dim3((unsigned)blocks, dst.batch), 256, 0, s>>>(src, dst));
   return GB_OK;
 }
 

@@ -13,8 +13,16 @@
 // The digits are computed from the FP64 bit pattern with integer arithmetic
 // only (GB300's FP64 ALU rate is ~1/64 of FP32).
 //
-// Plane layout: planes[b][s][r][kp] (bf16, row pitch kp = K rounded up to 8),
-// exponents exps[b][r] (int32).
+// Memory layout ("blocked"): the slices are stored in exactly the order the
+// tensor-core kernel's shared memory wants them, so that one pipeline stage of
+// one operand is a single contiguous bulk copy.  Rows are cut into blocks of
+// 128 and K into blocks of 16; block (rb, kb) holds the S slice tiles of
+// 128 x 16 bf16 back to back (4 KB each).  Inside a tile the 8 x 8 "core
+// matrices" (8 rows of 16 bytes) are ordered k group major, row group minor,
+// so the 16 core matrices of one k group are 2 KB of consecutive bytes:
+//   byte(r, k) = ((k / 8) * 16 + r / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
+// Blocks are ordered [batch][rb][kb].  Rows and K are zero-padded to whole
+// blocks.  Exponents: exps[b][r] (int32).
 #pragma once
 
 #include <cuda_bf16.h>
@@ -22,6 +30,10 @@
 #include "gemm_f64.cuh"
 
 namespace gb {
+
+constexpr int SL_ROWS = 128;               // rows per block
+constexpr int SL_K = 16;                   // K per block
+constexpr int SL_TILE_BYTES = SL_ROWS * SL_K * 2;  // one slice of one block: 4 KB
 
 struct SliceSrc {
   const double* p;
@@ -31,16 +43,28 @@ struct SliceSrc {
 };
 
 struct SlicedDesc {
-  __nv_bfloat16* planes;  // [batch][S][rows][kpad]
+  __nv_bfloat16* planes;  // blocked digit tiles
   int* exps;              // [batch][rows]
-  int batch, rows, K, kpad, S;
+  int batch, rows, K, S;
+  __host__ __device__ int rblocks() const { return (rows + SL_ROWS - 1) / SL_ROWS; }
+  __host__ __device__ int kblocks() const { return (K + SL_K - 1) / SL_K; }
+  __host__ __device__ long long block_bytes() const { return (long long)S * SL_TILE_BYTES; }
+  __host__ __device__ long long batch_bytes() const { return (long long)rblocks() * kblocks() * block_bytes(); }
 };
 
-inline int slice_kpad(int K) { return (K + 7) & ~7; }
 inline size_t sliced_plane_bytes(int batch, int rows, int K, int S) {
-  return (size_t)batch * S * rows * slice_kpad(K) * sizeof(__nv_bfloat16);
+  SlicedDesc d{nullptr, nullptr, batch, rows, K, S};
+  return (size_t)batch * d.batch_bytes();
 }
 inline size_t sliced_exp_bytes(int batch, int rows) { return (size_t)batch * rows * sizeof(int); }
+
+// Carve a sliced operand (planes + exponents) out of a workspace or buffer.
+template <class Cv>
+SlicedDesc take_sliced(Cv& c, int batch, int rows, int K, int S) {
+  auto* p = c.template take<unsigned char>(sliced_plane_bytes(batch, rows, K, S));
+  auto* e = c.template take<int>((size_t)batch * rows);
+  return SlicedDesc{reinterpret_cast<__nv_bfloat16*>(p), e, batch, rows, K, S};
+}
 
 // Exponents then digits; both kernels read the source once.
 int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s);
