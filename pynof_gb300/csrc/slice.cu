@@ -14,8 +14,12 @@ __device__ __forceinline__ int exponent_of(unsigned long long maxbits) {
   return (ex == 0 ? 1 : ex) - 1022;
 }
 
-// Balanced base-128 digits of round(x 2^(7S - E)), stored pre-weighted.
-__device__ __forceinline__ void make_digits(double x, int E, int S, __nv_bfloat16* out) {
+// Balanced base-128 digits of round(x 2^(7S - E)), stored pre-weighted as bf16
+// bit patterns.  Every digit value d 2^(-7 s) (|d| <= 128) is exact in bf16, so
+// its bf16 bits are the upper half of its FP32 bits; FP32 values come from
+// the integer with the 1.5 * 2^23 magic-number trick (exact for |d| < 2^22).
+template <int S>
+__device__ __forceinline__ void make_digits(double x, int E, unsigned short* out) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   int ex = (int)((bits >> 52) & 0x7FF);
   unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
@@ -26,17 +30,15 @@ __device__ __forceinline__ void make_digits(double x, int E, int S, __nv_bfloat1
   else if (r >= 64) xi = 0;
   else xi = (long long)((m + (1ull << (r - 1))) >> r);
   if (bits >> 63) xi = -xi;
-  float w = 1.0f;
-#pragma unroll 1
-  for (int s = 0; s < S; ++s) w *= 0.0078125f;  // 2^(-7S)
-#pragma unroll 1
+#pragma unroll
   for (int s = S; s >= 2; --s) {
-    const long long d = ((xi + 64) & 127) - 64;
+    const int d = (((int)xi + 64) & 127) - 64;
     xi = (xi - d) >> 7;
-    out[s - 1] = __float2bfloat16_rn((float)d * w);
-    w *= 128.0f;
+    const float f = (__int_as_float(0x4B400000 + d) - 12582912.0f) * __int_as_float((127 - 7 * s) << 23);
+    out[s - 1] = (unsigned short)(__float_as_uint(f) >> 16);
   }
-  out[0] = __float2bfloat16_rn((float)xi * w);
+  const float f1 = (__int_as_float(0x4B400000 + (int)xi) - 12582912.0f) * __int_as_float((127 - 7) << 23);
+  out[0] = (unsigned short)(__float_as_uint(f1) >> 16);
 }
 
 // One warp per row; K is the unit-stride index.
@@ -79,6 +81,7 @@ __global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restri
 // matrices (512 contiguous bytes) per slice, written with 16-byte stores; it
 // reads 64 contiguous source bytes per row (K-fast sources) or 256 contiguous
 // bytes per k (row-fast sources).
+template <int S>
 __global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, SlicedDesc dst) {
   const long long b = blockIdx.y;
   const int kbn = dst.kblocks();
@@ -87,26 +90,27 @@ __global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, Slice
   const int ri = lane & 7, kg = warp >> 2, rg = (warp & 3) * 4 + (lane >> 3);
   const int r = rb * SL_ROWS + rg * 8 + ri;
   const int k0 = kb * SL_K + kg * 8;
-  const int S = dst.S;
-  __nv_bfloat16 dg[8][6];
+  unsigned short dg[8][S];
   const bool rok = r < dst.rows;
   const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
   const int e = rok ? dst.exps[b * dst.rows + r] : 0;
+  double xs[8];
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
     const int k = k0 + u;
-    const double x = (rok && k < dst.K) ? base[src.k.at(k)] : 0.0;
-    make_digits(x, e, S, dg[u]);
+    xs[u] = (rok && k < dst.K) ? base[src.k.at(k)] : 0.0;
   }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) make_digits<S>(xs[u], e, dg[u]);
   unsigned char* out = reinterpret_cast<unsigned char*>(dst.planes) + b * dst.batch_bytes() +
                        ((long long)blockIdx.x * S) * SL_TILE_BYTES + (kg * 16 + rg) * 128 + ri * 16;
+#pragma unroll
   for (int s = 0; s < S; ++s) {
     uint4 v;
-    __nv_bfloat162 t;
-    t.x = dg[0][s]; t.y = dg[1][s]; v.x = *reinterpret_cast<unsigned*>(&t);
-    t.x = dg[2][s]; t.y = dg[3][s]; v.y = *reinterpret_cast<unsigned*>(&t);
-    t.x = dg[4][s]; t.y = dg[5][s]; v.z = *reinterpret_cast<unsigned*>(&t);
-    t.x = dg[6][s]; t.y = dg[7][s]; v.w = *reinterpret_cast<unsigned*>(&t);
+    v.x = (unsigned)dg[0][s] | ((unsigned)dg[1][s] << 16);
+    v.y = (unsigned)dg[2][s] | ((unsigned)dg[3][s] << 16);
+    v.z = (unsigned)dg[4][s] | ((unsigned)dg[5][s] << 16);
+    v.w = (unsigned)dg[6][s] | ((unsigned)dg[7][s] << 16);
     *reinterpret_cast<uint4*>(out + (long long)s * SL_TILE_BYTES) = v;
   }
 }
@@ -130,7 +134,15 @@ int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
   }
   const long long blocks = (long long)dst.rblocks() * dst.kblocks();
   GB_REQUIRE(blocks <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many blocks");
-  GB_LAUNCH("slice_digits", s, digits_blocked_kernel<<<dim3((unsigned)blocks, dst.batch), 256, 0, s>>>(src, dst));
+  const dim3 grid((unsigned)blocks, dst.batch);
+  switch (dst.S) {
+    case 1: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<1><<<grid, 256, 0, s>>>(src, dst)); break;
+    case 2: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<2><<<grid, 256, 0, s>>>(src, dst)); break;
+    case 3: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<3><<<grid, 256, 0, s>>>(src, dst)); break;
+    case 4: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<4><<<grid, 256, 0, s>>>(src, dst)); break;
+    case 5: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<5><<<grid, 256, 0, s>>>(src, dst)); break;
+    default: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<6><<<grid, 256, 0, s>>>(src, dst)); break;
+  }
   return GB_OK;
 }
 
