@@ -118,6 +118,59 @@ int gb_lagrange2_ri_f64(const double* C, const double* H, const double* b, const
                         int nalpha, double* elag, double* Hmat, void* workspace, size_t workspace_bytes,
                         void* stream);
 
+/* ------------------------------------------------------------------------
+ * A2  computeJKj, full ERI.  Replaces JKj_Full_GPU (pynof/integrals.py:221-231).
+ *     J_i[m][n] = sum_sl D_i[s][l] (mn|sl),  K_i[m][s] = sum_nl D_i[n][l] (mn|sl),
+ *     D_i = C_i C_i^T.  I is [nbf]^4 (8-fold symmetric).
+ * ---------------------------------------------------------------------- */
+size_t gb_jkj_full_workspace_f64(int nbf, int nbf5);
+int gb_jkj_full_f64(const double* C, const double* I, int nbf, int nbf5, double* J, double* K, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/* A4  computeJKH_MO, full ERI.  Replaces JKH_MO_Full_GPU (pynof/integrals.py:365-380). */
+size_t gb_jkh_mo_full_workspace_f64(int nbf, int nbf5);
+int gb_jkh_mo_full_f64(const double* C, const double* H, const double* I, int nbf, int nbf5, double* J_MO,
+                       double* K_MO, double* H_core, void* workspace, size_t workspace_bytes, void* stream);
+
+/* A6  Integrals_MO_Full.  Replaces Integrals_MO_Full_GPU (pynof/integrals.py:693-698).
+ *     Hmat [nbf][nbf5];  I_MO [nbf][nbf5][nbf5][nbf5] = (C^T, C_p^T, C_p^T, C_p^T) . I */
+size_t gb_mo_full_workspace_f64(int nbf, int nbf5);
+int gb_mo_full_f64(const double* C, const double* H, const double* I, int nbf, int nbf5, double* Hmat,
+                   double* I_MO, void* workspace, size_t workspace_bytes, void* stream);
+
+/* A6  computeLagrange2, full ERI, closed shell (pynof/utils.py:302-326).  The
+ *     diagonals of cj12 / ck12 are ignored. */
+size_t gb_lagrange2_full_workspace_f64(int nbf, int nbf5);
+int gb_lagrange2_full_f64(const double* C, const double* H, const double* I, const double* n, const double* cj12,
+                          const double* ck12, int nbf, int nbf5, int nbeta, int nalpha, double* elag, double* Hmat,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * A8  computeF_RC (closed shell).  Replaces computeF_RC_GPU
+ *     (pynof/utils.py:58-84).  F [nbf5][nbf][nbf];
+ *     F_i = n_i H + n_i J_i [ini <= i < nbeta or nalpha <= i] + sum_j cj12_ij J_j
+ *           - sum_j ck12_ij K_j, with ini = no1 if no1 > 1 else 0 and the
+ *     diagonal entries (i, i), i >= ini, of cj12 / ck12 ignored.
+ * ---------------------------------------------------------------------- */
+size_t gb_fock_rc_workspace_f64(int nbf, int nbf5);
+int gb_fock_rc_f64(const double* J, const double* K, const double* n, const double* H, const double* cj12,
+                   const double* ck12, int nbf, int nbf5, int nbeta, int nalpha, int no1, double* F, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* A8  computeLagrange (pynof/utils.py:249-259):
+ *     elag[k][i] = sum_mn C[m][k] F_i[m][n] C[n][i] for k < noptorb, i < nbf5; 0 elsewhere. */
+size_t gb_lagrange_workspace_f64(int nbf, int nbf5);
+int gb_lagrange_f64(const double* F, const double* C, int nbf, int nbf5, int noptorb, double* elag,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* A7  computeE_elec (pynof/utils.py:385-402): *E (device scalar) =
+ *     tr(elag[:nbf5, :nbf5]) + sum_i w_i C_i^T H C_i, w_i = n_i (1/2 for
+ *     nbeta <= i < nalpha when high_spin). */
+size_t gb_energy_elec_workspace_f64(int nbf, int nbf5);
+int gb_energy_elec_f64(const double* elag, const double* C, const double* H, const double* n, int nbf, int nbf5,
+                       int nbeta, int nalpha, int high_spin, double* E, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
 /* ========================================================================
  * Split-product ("mixed") path on the tcgen05 tensor cores.
  *

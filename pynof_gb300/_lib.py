@@ -45,6 +45,20 @@ SIGNATURES = {
     "gb_mo_ri_f64": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P, _Z, _P]),
     "gb_lagrange2_ri_workspace_f64": (_Z, [_I, _I, _I]),
     "gb_lagrange2_ri_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_jkj_full_workspace_f64": (_Z, [_I, _I]),
+    "gb_jkj_full_f64": (_I, [_P, _P, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_jkh_mo_full_workspace_f64": (_Z, [_I, _I]),
+    "gb_jkh_mo_full_f64": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _P, _Z, _P]),
+    "gb_mo_full_workspace_f64": (_Z, [_I, _I]),
+    "gb_mo_full_f64": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_lagrange2_full_workspace_f64": (_Z, [_I, _I]),
+    "gb_lagrange2_full_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_fock_rc_workspace_f64": (_Z, [_I, _I]),
+    "gb_fock_rc_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_lagrange_workspace_f64": (_Z, [_I, _I]),
+    "gb_lagrange_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_energy_elec_workspace_f64": (_Z, [_I, _I]),
+    "gb_energy_elec_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
     "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
     "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),

@@ -1,0 +1,86 @@
+"""Install the GB300 path into an imported ``pynof`` package.
+
+PyNOF resolves its contraction functions through module attributes at call
+time (``pynof.computeJKj``, ``pynof.integrals.JKj_RI_GPU``, ...), so
+rebinding those attributes makes every caller -- ``compute_energy``,
+``occoptr``, ``orbopt_adam``, ``calcorbe`` / ``calcorbg``, ``hfidr`` -- use the
+CUDA kernels when ``p.gpu`` is set, with ``param`` and every signature
+unchanged.  The dispatchers keep the reference's CPU branches for
+``p.gpu = False``.
+"""
+from __future__ import annotations
+
+from . import integrals, integrals_full, utils
+
+#: (module attribute path in pynof, replacement) for the p.gpu branches
+GPU_FUNCTIONS = {
+    "integrals.JKj_RI_GPU": integrals.JKj_RI_GPU,
+    "integrals.JKj_Full_GPU": integrals_full.JKj_Full_GPU,
+    "integrals.JKH_MO_RI_GPU": integrals.JKH_MO_RI_GPU,
+    "integrals.JKH_MO_Full_GPU": integrals_full.JKH_MO_Full_GPU,
+    "integrals.Integrals_MO_RI_GPU": integrals.Integrals_MO_RI_GPU,
+    "integrals.Integrals_MO_Full_GPU": integrals_full.Integrals_MO_Full_GPU,
+    "utils.computeF_RC_GPU": utils.computeF_RC_GPU,
+}
+
+
+def _gpu_or_cpu(gpu_fn, cpu_fn):
+    def dispatch(*args):
+        p = args[-1]
+        return gpu_fn(*args) if getattr(p, "gpu", False) else cpu_fn(*args)
+
+    dispatch.__name__ = getattr(cpu_fn, "__name__", "dispatch")
+    dispatch.__doc__ = f"p.gpu -> pynof_gb300, else the reference's {dispatch.__name__}"
+    return dispatch
+
+
+def install(pynof) -> dict:
+    """Rebind the GPU entry points of an imported ``pynof`` package.
+
+    Returns the previous bindings ({dotted name: object}) so that
+    :func:`uninstall` can restore them.
+    """
+    saved = {}
+    for dotted, fn in GPU_FUNCTIONS.items():
+        modname, attr = dotted.split(".")
+        mod = getattr(pynof, modname)
+        saved[dotted] = getattr(mod, attr)
+        setattr(mod, attr, fn)
+        if hasattr(pynof, attr):
+            saved["pynof." + attr] = getattr(pynof, attr)
+            setattr(pynof, attr, fn)
+    # compute_integrals uploads b_mnl / I with cupy (integrals.py:51-53): run it
+    # host-side and keep the tensors resident as CUDA tensors instead
+    orig_ci = pynof.integrals.compute_integrals
+
+    def compute_integrals(wfn, mol, p):
+        gpu = p.gpu
+        p.gpu = False
+        try:
+            S, T, V, H, I, b_mnl, Dipole = orig_ci(wfn, mol, p)
+        finally:
+            p.gpu = gpu
+        if gpu:
+            I, b_mnl = integrals.upload_integrals(I, b_mnl)
+        return S, T, V, H, I, b_mnl, Dipole
+
+    saved["integrals.compute_integrals"] = orig_ci
+    saved["pynof.compute_integrals"] = getattr(pynof, "compute_integrals", orig_ci)
+    pynof.integrals.compute_integrals = compute_integrals
+    pynof.compute_integrals = compute_integrals
+    # computeLagrange2 and ENERGY1r hold cupy code inline (utils.py:272-327),
+    # so they are replaced whole; the reference CPU branch stays behind p.gpu=False
+    for name, gpu_fn in (("computeLagrange2", utils.computeLagrange2), ("ENERGY1r", utils.ENERGY1r)):
+        cpu_fn = getattr(pynof.utils, name)
+        saved["utils." + name] = cpu_fn
+        saved["pynof." + name] = getattr(pynof, name)
+        disp = _gpu_or_cpu(gpu_fn, cpu_fn)
+        setattr(pynof.utils, name, disp)
+        setattr(pynof, name, disp)
+    return saved
+
+
+def uninstall(pynof, saved: dict) -> None:
+    for dotted, obj in saved.items():
+        modname, attr = dotted.split(".")
+        setattr(pynof if modname == "pynof" else getattr(pynof, modname), attr, obj)

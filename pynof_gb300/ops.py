@@ -154,6 +154,118 @@ def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
 
 
 # ----------------------------------------------------------------------------
+# full-ERI path (A2, A4, A6)
+# ----------------------------------------------------------------------------
+def jkj_full(C, I, nbf5: int):
+    """J, K (nbf5, nbf, nbf) from the 4-index tensor (A2)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    _require(I, (N, N, N, N), "I")
+    dev = I.device
+    J = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    K = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_jkj_full_workspace_f64", N, nbf5, device=dev)
+    _lib.call("gb_jkj_full_f64", _ptr(C), _ptr(I), N, nbf5, _ptr(J), _ptr(K), wp, wn, _stream(dev))
+    return J, K
+
+
+def jkh_mo_full(C, H, I, nbf5: int):
+    """J_MO, K_MO, H_core from the 4-index tensor (A4)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(I, (N, N, N, N), "I")
+    dev = I.device
+    J_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    K_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    H_core = torch.empty((nbf5,), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_jkh_mo_full_workspace_f64", N, nbf5, device=dev)
+    _lib.call("gb_jkh_mo_full_f64", _ptr(C), _ptr(H), _ptr(I), N, nbf5, _ptr(J_MO), _ptr(K_MO), _ptr(H_core), wp, wn,
+              _stream(dev))
+    return J_MO, K_MO, H_core
+
+
+def mo_full(C, H, I, nbf5: int):
+    """Hmat (nbf, nbf5), I_MO (nbf, nbf5, nbf5, nbf5) (A6)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(I, (N, N, N, N), "I")
+    dev = I.device
+    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    imo = torch.empty((N, nbf5, nbf5, nbf5), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_mo_full_workspace_f64", N, nbf5, device=dev)
+    _lib.call("gb_mo_full_f64", _ptr(C), _ptr(H), _ptr(I), N, nbf5, _ptr(Hmat), _ptr(imo), wp, wn, _stream(dev))
+    return Hmat, imo
+
+
+def lagrange2_full(C, H, I, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
+    """elag (nbf, nbf), Hmat (nbf, nbf5) from the 4-index tensor (A6)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(I, (N, N, N, N), "I")
+    _require(n, (nbf5,), "n")
+    _require(cj12, (nbf5, nbf5), "cj12")
+    _require(ck12, (nbf5, nbf5), "ck12")
+    dev = I.device
+    elag = torch.empty((N, N), dtype=_F64, device=dev)
+    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_lagrange2_full_workspace_f64", N, nbf5, device=dev)
+    _lib.call("gb_lagrange2_full_f64", _ptr(C), _ptr(H), _ptr(I), _ptr(n), _ptr(cj12), _ptr(ck12), N, nbf5, nbeta,
+              nalpha, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
+    return elag, Hmat
+
+
+# ----------------------------------------------------------------------------
+# AO route: generalized Fock, Lagrangian, energy (A8, A7)
+# ----------------------------------------------------------------------------
+def fock_rc(J, K, n, H, cj12, ck12, nbeta: int, nalpha: int, no1: int = 0):
+    """F (nbf5, nbf, nbf), closed shell (computeF_RC)."""
+    P, N, _ = J.shape
+    _require(J, (P, N, N), "J")
+    _require(K, (P, N, N), "K")
+    _require(n, (P,), "n")
+    _require(H, (N, N), "H")
+    _require(cj12, (P, P), "cj12")
+    _require(ck12, (P, P), "ck12")
+    dev = J.device
+    F = torch.empty((P, N, N), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_fock_rc_workspace_f64", N, P, device=dev)
+    _lib.call("gb_fock_rc_f64", _ptr(J), _ptr(K), _ptr(n), _ptr(H), _ptr(cj12), _ptr(ck12), N, P, nbeta, nalpha, no1,
+              _ptr(F), wp, wn, _stream(dev))
+    return F
+
+
+def lagrange(F, C, noptorb: int | None = None):
+    """elag (nbf, nbf) from the generalized Fock matrices (computeLagrange)."""
+    P, N, _ = F.shape
+    _require(F, (P, N, N), "F")
+    _require(C, (N, N), "C")
+    dev = F.device
+    elag = torch.empty((N, N), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_lagrange_workspace_f64", N, P, device=dev)
+    _lib.call("gb_lagrange_f64", _ptr(F), _ptr(C), N, P, noptorb or N, _ptr(elag), wp, wn, _stream(dev))
+    return elag
+
+
+def energy_elec(elag, C, H, n, nbeta: int, nalpha: int, high_spin: bool = False):
+    """Electronic energy (computeE_elec) as a 0-d CUDA tensor."""
+    N = C.shape[0]
+    P = n.shape[0]
+    _require(elag, (N, N), "elag")
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(n, (P,), "n")
+    dev = C.device
+    E = torch.empty((), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_energy_elec_workspace_f64", N, P, device=dev)
+    _lib.call("gb_energy_elec_f64", _ptr(elag), _ptr(C), _ptr(H), _ptr(n), N, P, nbeta, nalpha, int(high_spin),
+              _ptr(E), wp, wn, _stream(dev))
+    return E
+
+
+# ----------------------------------------------------------------------------
 # split-product tensor-core path
 # ----------------------------------------------------------------------------
 def check_device_status() -> None:
