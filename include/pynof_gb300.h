@@ -208,6 +208,21 @@ size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
 int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
                     double* K, void* workspace, size_t workspace_bytes, void* stream);
 
+/* A3  computeJKH_MO, RI, on the tensor cores (same outputs as gb_jkh_mo_ri_f64).
+ *     Replaces JKH_MO_RI_GPU (pynof/integrals.py:383-399). */
+size_t gb_jkh_mo_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
+int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* prep, int nbf, int nbf5, int naux, int nslices,
+                       double* J_MO, double* K_MO, double* H_core, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* A5  computeLagrange2, RI, closed shell, on the tensor cores (same outputs as
+ *     gb_lagrange2_ri_f64; relies on the (m, n) symmetry of b).  Replaces the
+ *     GPU branch of computeLagrange2 (pynof/utils.py:262-327). */
+size_t gb_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
+int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n, const double* cj12,
+                          const double* ck12, int nbf, int nbf5, int naux, int nbeta, int nalpha, int nslices,
+                          double* elag, double* Hmat, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

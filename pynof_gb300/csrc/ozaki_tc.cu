@@ -274,9 +274,11 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
     if (lane == 0) {
       int issued = 0;
       const uint32_t half = (uint32_t)S * TILE_BYTES;
-      const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + (long long)bz * a.A.batch_bytes() +
+      // an operand sliced once (batch 1) is shared by every batch entry
+      const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
+      const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
                                 (long long)(m0 / BM) * a.A.kblocks() * half;
-      const unsigned char* gb_ = reinterpret_cast<const unsigned char*>(a.B.planes) + (long long)bz * a.B.batch_bytes() +
+      const unsigned char* gb_ = reinterpret_cast<const unsigned char*>(a.B.planes) + bbz * a.B.batch_bytes() +
                                  (long long)(n0 / BN) * a.B.kblocks() * half;
       for (int kb = 0; kb < nkb; ++kb) {
         const int st = kb % STAGES;
@@ -310,15 +312,28 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
         tc_fence_after();
         const uint32_t sa = sbase + st * stage_bytes;
         const uint64_t da = desc_tile(sa), db = desc_tile(sa + S * TILE_BYTES);
-        if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
         const int c = kb / CH;
         const bool first = (kb % CH) == 0;
-        if (first && c > 0) {
-          if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
-            signal_abort(abort_flag);
-            break;
+        if (g.fdrain) {
+          // the FP32 accumulator is drained with the exact groups: restart it every chunk
+          if (first && c > 0) {
+            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
+              signal_abort(abort_flag);
+              break;
+            }
+            tc_fence_after();
           }
-          tc_fence_after();
+          if (first) f_started = false;
+          if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
+        } else {
+          if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
+          if (first && c > 0) {
+            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
+              signal_abort(abort_flag);
+              break;
+            }
+            tc_fence_after();
+          }
         }
         issue_exact<S>(tmem, da, db, first);
         if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(accfull_bar);
@@ -343,9 +358,10 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
         break;
       }
       tc_fence_after();
+      const int fr = g.fdrain ? a.frac : 0;  // fraction bits carried by R from the start
       for (int gg = 2; gg <= gE; ++gg) {
         const float up = __int_as_float((127 + 7 * gg) << 23);  // 2^(7 g)
-        const int sh = 7 * (gE - gg);
+        const int sh = 7 * (gE - gg) + fr;
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           uint32_t v[8];
@@ -356,6 +372,16 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
             const long long iv = (long long)(__float_as_int(f) - MAGIC_BITS);
             R[h * 8 + j] += (long long)((unsigned long long)iv << sh);
           }
+        }
+      }
+      if (has_inexact && g.fdrain) {
+        const float upEF = __int_as_float((127 + 7 * gE + a.frac) << 23);  // 2^(7 gE + frac)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          uint32_t v[8];
+          tmem_ld8(lbase + 384u + (uint32_t)(h * 8), v);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) R[h * 8 + j] += __float2ll_rn(__uint_as_float(v[j]) * upEF);
         }
       }
       tc_fence_before();
@@ -374,14 +400,14 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
       const int i = m0 + q * 32 + lane;
       const float upE = __int_as_float((127 + 7 * gE) << 23);
       const float upF = __int_as_float((127 + a.frac) << 23);
-      const int ea = (i < g.M) ? a.A.exps[(long long)bz * g.M + i] : 0;
+      const int ea = (i < g.M) ? a.A.exps[(a.A.batch == 1 ? 0LL : (long long)bz) * g.M + i] : 0;
       double* Cb = g.C + (long long)bz * g.c_sb;
       const long long ri = (i < g.M) ? g.c_r.at(i) : 0;
       const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
         uint32_t v[8];
-        if (has_inexact) {
+        if (has_inexact && !g.fdrain) {
           tmem_ld8(lbase + 384u + (uint32_t)(h * 8), v);
         } else {
 #pragma unroll
@@ -395,8 +421,9 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
           const float th = rintf(t);
           const long long hi = __float2ll_rn(th);
           const long long lo = __float2ll_rn((t - th) * upF);
-          const long long z = (long long)((unsigned long long)(R[h * 8 + j] + hi) << a.frac) + lo;
-          const int eb = a.B.exps[(long long)bz * g.N + jj];
+          const long long z = g.fdrain ? R[h * 8 + j]
+                                       : (long long)((unsigned long long)(R[h * 8 + j] + hi) << a.frac) + lo;
+          const int eb = a.B.exps[(a.B.batch == 1 ? 0LL : (long long)bz) * g.N + jj];
           const double val = fixed_to_double(z, ea + eb - 7 * gE - a.frac, g.negate);
           Cb[ri + g.c_c.at(jj)] = val;
           if (mirror_rc) {
@@ -443,8 +470,8 @@ KernelFn kernel_for(int S) {
 int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaStream_t stream) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return GB_OK;
   GB_REQUIRE(g.S >= 1 && g.S <= 6 && A.S == g.S && B.S == g.S, GB_ERR_INVALID_ARG, "ozaki_gemm: nslices mismatch");
-  GB_REQUIRE(A.rows == g.M && B.rows == g.N && A.K == g.K && B.K == g.K && A.batch == g.batch &&
-                 B.batch == g.batch,
+  GB_REQUIRE(A.rows == g.M && B.rows == g.N && A.K == g.K && B.K == g.K && (A.batch == g.batch || A.batch == 1) &&
+                 (B.batch == g.batch || B.batch == 1),
              GB_ERR_BAD_SHAPE, "ozaki_gemm: operand shapes do not match the GEMM");
   GB_REQUIRE(g.sym != SYM_ROWCOL || g.M == g.N, GB_ERR_BAD_SHAPE, "ozaki_gemm: SYM_ROWCOL needs M == N");
   GB_REQUIRE(g.sym != SYM_PAIRCOL || (long long)g.pair_n * g.pair_n == g.N, GB_ERR_BAD_SHAPE,
@@ -482,6 +509,7 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   if (frac > 16) frac = 16;
   if (frac < 0) frac = 0;
   KArgs ka{g, A, B, frac};
+  if (g.K > 4096) ka.g.fdrain = 1;
   dim3 grid((unsigned)tiles, (unsigned)g.batch);
   const int pi = prof_begin(g.tag, stream);
   kernel_for(g.S)<<<grid, THREADS, smem, stream>>>(ka);

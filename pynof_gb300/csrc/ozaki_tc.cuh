@@ -30,6 +30,11 @@ struct OzGemm {
   Index2 c_r, c_c;
   int sym, pair_n;
   int negate;
+  // Drain the FP32 accumulator of the small slice groups into the int64 fixed
+  // point after every 192-k chunk (instead of once at the end): its rounding
+  // error then stops growing with K.  Costs the overlap of the drain with
+  // the MMAs; used for long contractions (K > 4096).
+  int fdrain = 0;
   const char* tag = "ozaki_tc";
 };
 

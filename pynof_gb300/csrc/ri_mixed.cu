@@ -5,6 +5,7 @@
 //   bT[j = (n, l)][m]  (K = m, for the half transform T = C_p^T b)
 //   bJ[j = (m, n)][l]  (K = l, for J = d b^T)
 // and stays resident across builds, like b itself in PyNOF's GPU path.
+#include "gemm_f64.cuh"
 #include "ozaki_tc.cuh"
 #include "ri_kernels.cuh"
 #include "slice.cuh"
@@ -188,4 +189,203 @@ extern "C" int gb_dgemm_mixed(const double* A, const double* B, int M, int N, in
   g.C = C; g.c_sb = 0; g.c_r = lin(N); g.c_c = lin(1);
   g.sym = SYM_NONE; g.tag = "ozaki_tc:dgemm";
   return ozaki_gemm(sa, sb, g, s);
+}
+
+// ---------------------------------------------------------------------------
+// A3  computeJKH_MO, RI, on the tensor cores
+//   T  = C_p^T b                   (half transform, as in the JK build)
+//   bpq[p][q][l] = sum_n C[n][q] T[p][n][l]   (batched over p; T read with K = n)
+//   J_MO = d d^T (d[p] = bpq[p][p]),  K_MO[p][q] = sum_l bpq[p][q][l]^2,  H_core
+// ---------------------------------------------------------------------------
+namespace {
+struct JkhMixedWs {
+  SlicedDesc A, Tt;
+  double *Tf, *bpq, *d, *X;
+};
+
+template <class Cv>
+void jkh_mixed_layout(Cv& c, int N, int P, int Q, int S, JkhMixedWs* w) {
+  SlicedDesc A = take_sliced(c, 1, P, N, S);
+  auto* tf = c.template take<double>((size_t)P * N * Q);
+  SlicedDesc Tt = take_sliced(c, P, Q, N, S);
+  auto* bpq = c.template take<double>((size_t)P * P * Q);
+  auto* d = c.template take<double>((size_t)P * Q);
+  auto* X = c.template take<double>((size_t)N * P);
+  if (w) *w = JkhMixedWs{A, Tt, tf, bpq, d, X};
+}
+
+// H_core[p] = C_p^T H C_p and (optionally) Hmat = C^T H C_p in FP64
+int hcore_f64(const double* C, const double* H, int N, int P, double* X, double* H_core, double* Hmat,
+              cudaStream_t s) {
+  GemmF64 g{};
+  g.M = N; g.N = P; g.K = N; g.batch = 1;
+  g.A = {H, 0, lin(N), lin(1)};
+  g.B = {C, 0, lin(N), lin(1)};
+  g.C = {X, 0, lin(P), lin(1)};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_NONE;
+  g.a_kfast = true; g.b_kfast = false;
+  g.tag = "gemm_f64:small";
+  GB_TRY(gemm_f64(g, s));
+  if (H_core) GB_TRY(launch_col_dot(C, N, X, P, H_core, N, P, s));
+  if (Hmat) {
+    g.A = {C, 0, lin(1), lin(N)};
+    g.B = {X, 0, lin(P), lin(1)};
+    g.C = {Hmat, 0, lin(P), lin(1)};
+    g.a_kfast = false; g.b_kfast = false;
+    GB_TRY(gemm_f64(g, s));
+  }
+  return GB_OK;
+}
+
+int half_transform_mixed(const double* C, const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q,
+                         double* Tf, cudaStream_t s) {
+  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, A, s));
+  OzGemm gt{};
+  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = A.S;
+  gt.C = Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
+  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
+  return ozaki_gemm(A, bT, gt, s);
+}
+}  // namespace
+
+extern "C" size_t gb_jkh_mo_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices) {
+  SizeCarve c;
+  jkh_mixed_layout(c, nbf, nbf5, naux, nslices, nullptr);
+  return c.used;
+}
+
+extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* prep, int nbf, int nbf5, int naux,
+                                  int nslices, double* J_MO, double* K_MO, double* H_core, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(check_mixed(N, P, Q, S));
+  GB_REQUIRE(C && H && prep && J_MO && K_MO && H_core, GB_ERR_INVALID_ARG, "gb_jkh_mo_ri_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_jkh_mo_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "gb_jkh_mo_ri_mixed: workspace too small");
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkhMixedWs w;
+  jkh_mixed_layout(wc, N, P, Q, S, &w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GB_TRY(half_transform_mixed(C, w.A, pr.bT, N, P, Q, w.Tf, s));
+  // T read with rows l and K = n: element T[p][n][l]
+  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
+  OzGemm gq{};
+  gq.M = P; gq.N = Q; gq.K = N; gq.batch = P; gq.S = S;
+  gq.C = w.bpq; gq.c_sb = (long long)P * Q; gq.c_r = lin(Q); gq.c_c = lin(1);
+  gq.sym = SYM_NONE; gq.tag = "ozaki_tc:bpq";
+  GB_TRY(ozaki_gemm(w.A, w.Tt, gq, s));
+  GB_TRY(launch_gather_diag(w.bpq, w.d, P, Q, (long long)P * Q + Q, s));
+  GemmF64 gj{};
+  gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1;
+  gj.A = {w.d, 0, lin(Q), lin(1)};
+  gj.B = {w.d, 0, lin(1), lin(Q)};
+  gj.C = {J_MO, 0, lin(P), lin(1)};
+  gj.alpha = 1.0; gj.beta = 0.0; gj.sym = SYM_ROWCOL;
+  gj.a_kfast = true; gj.b_kfast = true;
+  gj.tag = "gemm_f64:small";
+  GB_TRY(gemm_f64(gj, s));
+  GB_TRY(launch_row_sumsq(w.bpq, K_MO, (long long)P * P, Q, s));
+  return hcore_f64(C, H, N, P, w.X, H_core, nullptr, s);
+}
+
+// ---------------------------------------------------------------------------
+// A5  computeLagrange2, RI, closed shell, on the tensor cores
+//   bMO[a][q][l] = sum_m C[m][a] T[q][m][l]  (T[q][m][l] = sum_n C[n][q] b[m][n][l]
+//   equals the half transform because b is symmetric in (m, n))
+//   elag = -bMO . (ck12-weighted bMO)^T (K = nbf5 naux) + FP64 terms.
+// ---------------------------------------------------------------------------
+namespace {
+struct Lag2MixedWs {
+  SlicedDesc Aall, Tt, Sx, Sy;
+  double *Tf, *bMO, *Y, *X, *d, *w, *cjm;
+};
+
+template <class Cv>
+void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
+  SlicedDesc Aall = take_sliced(c, 1, N, N, S);
+  auto* tf = c.template take<double>((size_t)P * N * Q);
+  SlicedDesc Tt = take_sliced(c, P, Q, N, S);
+  auto* bmo = c.template take<double>((size_t)N * P * Q);
+  auto* Y = c.template take<double>((size_t)P * P * Q);
+  SlicedDesc Sx = take_sliced(c, 1, N, P * Q, S);
+  SlicedDesc Sy = take_sliced(c, 1, P, P * Q, S);
+  auto* X = c.template take<double>((size_t)N * P);
+  auto* d = c.template take<double>((size_t)P * Q);
+  auto* wv = c.template take<double>((size_t)P * Q);
+  auto* cjm = c.template take<double>((size_t)P * P);
+  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm};
+}
+}  // namespace
+
+extern "C" size_t gb_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices) {
+  SizeCarve c;
+  lag2_mixed_layout(c, nbf, nbf5, naux, nslices, nullptr);
+  return c.used;
+}
+
+extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n,
+                                     const double* cj12, const double* ck12, int nbf, int nbf5, int naux, int nbeta,
+                                     int nalpha, int nslices, double* elag, double* Hmat, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(check_mixed(N, P, Q, S));
+  GB_REQUIRE((long long)P * Q < 2147483647LL, GB_ERR_BAD_SHAPE, "gb_lagrange2_ri_mixed: nbf5*naux too large");
+  GB_REQUIRE(0 <= nbeta && nbeta <= nalpha && nalpha <= P, GB_ERR_BAD_SHAPE,
+             "gb_lagrange2_ri_mixed: need 0 <= nbeta <= nalpha <= nbf5");
+  GB_REQUIRE(C && H && prep && n && cj12 && ck12 && elag && Hmat, GB_ERR_INVALID_ARG,
+             "gb_lagrange2_ri_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_lagrange2_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "gb_lagrange2_ri_mixed: workspace too small");
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  Lag2MixedWs w;
+  lag2_mixed_layout(wc, N, P, Q, S, &w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  // C^T sliced once for all nbf rows; its first nbf5 rows are the half transform's A
+  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Aall, s));
+  SlicedDesc Ap = w.Aall;
+  Ap.rows = P;
+  OzGemm gt{};
+  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = S;
+  gt.C = w.Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
+  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
+  GB_TRY(ozaki_gemm(Ap, pr.bT, gt, s));
+  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
+  // bMO[a][q][l] (batch q)
+  OzGemm gm{};
+  gm.M = N; gm.N = Q; gm.K = N; gm.batch = P; gm.S = S;
+  gm.C = w.bMO; gm.c_sb = Q; gm.c_r = lin((long long)P * Q); gm.c_c = lin(1);
+  gm.sym = SYM_NONE; gm.tag = "ozaki_tc:bMO";
+  GB_TRY(ozaki_gemm(w.Aall, w.Tt, gm, s));
+  GB_TRY(hcore_f64(C, H, N, P, w.X, nullptr, Hmat, s));
+  GB_TRY(launch_gather_diag(w.bMO, w.d, P, Q, (long long)P * Q + Q, s));
+  GB_TRY(launch_copy_zero_diag(cj12, w.cjm, P, s));
+  GemmF64 gw{};
+  gw.M = P; gw.N = Q; gw.K = P; gw.batch = 1;
+  gw.A = {w.cjm, 0, lin(P), lin(1)};
+  gw.B = {w.d, 0, lin(Q), lin(1)};
+  gw.C = {w.w, 0, lin(Q), lin(1)};
+  gw.alpha = 1.0; gw.beta = 0.0; gw.sym = SYM_NONE;
+  gw.a_kfast = true; gw.b_kfast = false;
+  gw.tag = "gemm_f64:small";
+  GB_TRY(gemm_f64(gw, s));
+  GB_TRY(launch_add_scaled_rows(w.w, w.d, n, P, Q, nbeta, nalpha, s));
+  GB_TRY(launch_make_ck_weighted(w.bMO, ck12, w.Y, P, Q, s));
+  // elag[a][b] = -sum_(q,l) bMO[a][(q,l)] Y[b][(q,l)]
+  GB_TRY(slice_operand(SliceSrc{w.bMO, 0, lin((long long)P * Q), lin(1), true}, w.Sx, s));
+  GB_TRY(slice_operand(SliceSrc{w.Y, 0, lin((long long)P * Q), lin(1), true}, w.Sy, s));
+  OzGemm ge{};
+  ge.M = N; ge.N = P; ge.K = P * Q; ge.batch = 1; ge.S = S;
+  ge.C = elag; ge.c_sb = 0; ge.c_r = lin(N); ge.c_c = lin(1);
+  ge.sym = SYM_NONE; ge.negate = 1; ge.tag = "ozaki_tc:ck_exchange";
+  GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
+  return launch_lagrange2_finish(w.bMO, w.w, Hmat, n, elag, N, P, Q, s);
 }

@@ -125,10 +125,17 @@ def computeJKj(C, I, b_mnl, p):
 # ---------------------------------------------------------------------------
 # A3  computeJKH_MO
 # ---------------------------------------------------------------------------
+def jkh_mo_ri_device(C, H, b_mnl, nbf5):
+    """J_MO, K_MO, H_core as CUDA tensors with the arithmetic of ``PRECISION``."""
+    dC, dH, db = as_device(C), as_device(H), as_device(b_mnl)
+    if PRECISION["mode"] == "mixed":
+        return ops.jkh_mo_ri_mixed(dC, dH, prepared(db, PRECISION["nslices"]), nbf5)
+    return ops.jkh_mo_ri(dC, dH, db, nbf5)
+
+
 def JKH_MO_RI_GPU(C, H, b_mnl, p):
     """J_MO, K_MO (nbf5, nbf5), H_core (nbf5,) -- ``pynof/integrals.py:383-399``."""
-    a, b, c = ops.jkh_mo_ri(as_device(C), as_device(H), as_device(b_mnl), p.nbf5)
-    return to_host(a, b, c)
+    return to_host(*jkh_mo_ri_device(C, H, b_mnl, p.nbf5))
 
 
 def computeJKH_MO(C, H, I, b_mnl, p):

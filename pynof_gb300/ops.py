@@ -316,3 +316,35 @@ def jkj_ri_mixed(C: torch.Tensor, prep: PreparedRI, nbf5: int):
     _lib.call("gb_jkj_ri_mixed", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J), _ptr(K), wp, wn,
               _stream(dev))
     return J, K
+
+
+def jkh_mo_ri_mixed(C, H, prep: PreparedRI, nbf5: int):
+    """J_MO, K_MO, H_core on the tensor cores (A3)."""
+    N, Q, S = prep.nbf, prep.naux, prep.nslices
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    dev = prep.device
+    J_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    K_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
+    H_core = torch.empty((nbf5,), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_jkh_mo_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
+    _lib.call("gb_jkh_mo_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J_MO), _ptr(K_MO),
+              _ptr(H_core), wp, wn, _stream(dev))
+    return J_MO, K_MO, H_core
+
+
+def lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
+    """elag, Hmat on the tensor cores (A5, closed shell)."""
+    N, Q, S = prep.nbf, prep.naux, prep.nslices
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(n, (nbf5,), "n")
+    _require(cj12, (nbf5, nbf5), "cj12")
+    _require(ck12, (nbf5, nbf5), "ck12")
+    dev = prep.device
+    elag = torch.empty((N, N), dtype=_F64, device=dev)
+    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_lagrange2_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
+    _lib.call("gb_lagrange2_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), _ptr(n), _ptr(cj12), _ptr(ck12), N,
+              nbf5, Q, nbeta, nalpha, S, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
+    return elag, Hmat

@@ -31,7 +31,11 @@ def computeLagrange2_device(n, cj12, ck12, C, H, I, b_mnl, p):
         Hmat = ops.mo_ri(dC, dH, as_device(b_mnl), p.nbf5)[0] if p.RI else ops.mo_full(dC, dH, as_device(I), p.nbf5)[0]
         return torch.zeros((N, N), dtype=torch.float64, device=dC.device), Hmat
     if p.RI:
-        return ops.lagrange2_ri(dC, dH, as_device(b_mnl), dn, dcj, dck, p.nbf5, p.nbeta, p.nalpha)
+        db = as_device(b_mnl)
+        if PRECISION["mode"] == "mixed":
+            return ops.lagrange2_ri_mixed(dC, dH, prepared(db, PRECISION["nslices"]), dn, dcj, dck, p.nbf5, p.nbeta,
+                                          p.nalpha)
+        return ops.lagrange2_ri(dC, dH, db, dn, dcj, dck, p.nbf5, p.nbeta, p.nalpha)
     return ops.lagrange2_full(dC, dH, as_device(I), dn, dcj, dck, p.nbf5, p.nbeta, p.nalpha)
 
 

@@ -31,7 +31,8 @@ def test_dgemm_small_integers_exact(torch_cuda):
     assert np.array_equal(C, A @ B.T)
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 300, 500), (77, 130, 1000), (256, 384, 2400)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (200, 300, 500), (77, 130, 1000), (256, 384, 2400),
+                                   (130, 70, 30000)])
 def test_dgemm_random(torch_cuda, M, N, K):
     from pynof_gb300 import ops
 
@@ -83,3 +84,45 @@ def test_jkj_ri_mixed_vs_oracle(torch_cuda, N, Q, ndoc, ncwo, seed):
         print(f"jkj N={N} Q={Q} nslices={S}: J {nrel(J.cpu().numpy(), Jr):.2e} K {nrel(K.cpu().numpy(), Kr):.2e}")
         assert nrel(J.cpu().numpy(), Jr) < tol, (S, nrel(J.cpu().numpy(), Jr))
         assert nrel(K.cpu().numpy(), Kr) < tol, (S, nrel(K.cpu().numpy(), Kr))
+
+
+def test_jkh_mo_and_lagrange2_mixed_golden(case):
+    from pynof_gb300 import ops
+
+    g, p, d = case
+    prep = ops.PreparedRI(d["b"], nslices=6)
+    dH = ops.to_device(g["H"])
+    a, b, c = ops.jkh_mo_ri_mixed(d["C"], dH, prep, p.nbf5)
+    ops.check_device_status()
+    assert nrel(a.cpu().numpy(), g["J_MO_ri"]) < 1e-10
+    assert nrel(b.cpu().numpy(), g["K_MO_ri"]) < 1e-10
+    assert nrel(c.cpu().numpy(), g["H_core"]) < 1e-10
+    el, Hm = ops.lagrange2_ri_mixed(d["C"], dH, prep, ops.to_device(g["n_soft"]), ops.to_device(g["cj12"]),
+                                    ops.to_device(g["ck12"]), p.nbf5, p.nbeta, p.nalpha)
+    ops.check_device_status()
+    assert nrel(el.cpu().numpy(), g["elag2_ri"]) < 1e-10
+    assert nrel(Hm.cpu().numpy(), g["Hmat"]) < 1e-10
+
+
+def test_jkh_mo_and_lagrange2_mixed_vs_oracle(torch_cuda):
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import ops, synthetic
+
+    st = synthetic.Structure(nbf=150, nbfaux=600, ndoc=15, ncwo=4)
+    b, C, H, n = synthetic.make_inputs(st, 8)
+    P = st.nbf5
+    db, dC, dH = ops.to_device(b), ops.to_device(C), ops.to_device(H)
+    cj = 2 * np.outer(n, n)
+    ck = np.outer(n, n) + 0.1
+    ar, br, cr = orc.jkh_mo_ri(C, H, b, P)
+    elr, Hr = orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st)
+    for S, tol in ((6, 1e-10), (2, 1e-3)):
+        prep = ops.PreparedRI(db, nslices=S)
+        a, bb, c = ops.jkh_mo_ri_mixed(dC, dH, prep, P)
+        el, Hm = ops.lagrange2_ri_mixed(dC, dH, prep, ops.to_device(n), ops.to_device(cj), ops.to_device(ck), P,
+                                        st.nbeta, st.nalpha)
+        ops.check_device_status()
+        errs = [nrel(a.cpu().numpy(), ar), nrel(bb.cpu().numpy(), br), nrel(el.cpu().numpy(), elr)]
+        print(f"nslices={S}: J_MO {errs[0]:.2e} K_MO {errs[1]:.2e} elag {errs[2]:.2e}")
+        assert max(errs) < tol, (S, errs)
+        assert nrel(c.cpu().numpy(), cr) < 1e-12 and nrel(Hm.cpu().numpy(), Hr) < 1e-12
