@@ -40,12 +40,21 @@ def ocupacion_softmax(gamma, p):
     n = np.zeros(p.nbf5)
     dn = np.zeros((p.nbf5, p.nv))
     n[p.no1 + p.ndoc: p.no1 + p.ndns] = 1.0 if p.HighSpin else 0.5
-    ex = np.exp(gamma)
     for i, (_, weak, gam) in enumerate(_pairs(p)):
-        e = ex[gam]
-        den = 1.0 + e.sum()
-        ns = 1.0 / den
-        nw = e / den
+        x = gamma[gam]
+        top = x.max() if len(x) else 0.0
+        if top < 700.0:
+            e = np.exp(x)
+            den = 1.0 + e.sum()
+            ns = 1.0 / den
+            nw = e / den
+        else:
+            # logits a line search pushed past exp's range: the same softmax,
+            # shifted by its largest logit
+            e = np.exp(x - top)
+            den = np.exp(-top) + e.sum()
+            ns = np.exp(-top) / den
+            nw = e / den
         # the reference writes the strong occupation at index i (pnof.py:793)
         n[i] = ns
         n[weak] = nw

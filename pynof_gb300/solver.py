@@ -1,0 +1,216 @@
+"""psi4-free NOF solve loop over the device kernels.
+
+Restates the orbital / occupation optimisation of ``pynof.compute_energy``
+(``energy.py:94-170``) -- ``occoptr`` (``minimization.py:77-97``, scipy CG
+over the softmax gammas), ``orbopt_adam`` (``minimization.py:200-253``,
+AMSgrad on orbital rotations), ``order_occupations_softmax``
+(``guess.py:77-106``) and the convergence test on the two gradient norms --
+with every four-index contraction (``computeJKH_MO``, ``computeLagrange2``) on
+the GPU and the occupation-space / rotation math in FP64 on the host
+(:mod:`pynof_gb300.nof`).
+
+A :class:`Backend` owns one molecule's resident device state (b, its sliced
+form for the tensor-core path, H) and a CUDA stream, so several solves can
+run concurrently (the serving loop).
+"""
+from __future__ import annotations
+
+import copy
+import dataclasses
+import time
+
+import numpy as np
+import scipy.optimize
+import torch
+
+from . import integrals, nof, ops
+
+
+class Backend:
+    """Device contractions for one molecule.
+
+    precision: "fp64" (DMMA) or "mixed" (tcgen05 digit slices, ``nslices``)."""
+
+    def __init__(self, st, b, H, precision: str = "mixed", nslices: int = 6, device=None, stream=None):
+        self.st = st
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.stream = stream if stream is not None else torch.cuda.Stream(self.device)
+        self.precision = precision
+        self.nslices = nslices
+        with torch.cuda.stream(self.stream):
+            self.b = ops.to_device(b, self.device)
+            self.H = ops.to_device(H, self.device)
+            self.prep = ops.PreparedRI(self.b, nslices) if precision == "mixed" else None
+        self.calls = {"jkh_mo": 0, "lagrange2": 0}
+
+    def set_precision(self, precision: str, nslices: int | None = None):
+        """Switch arithmetic (e.g. to FP64 near convergence)."""
+        self.precision = precision
+        if nslices is not None and nslices != self.nslices:
+            self.nslices = nslices
+            self.prep = None
+        if precision == "mixed" and self.prep is None:
+            with torch.cuda.stream(self.stream):
+                self.prep = ops.PreparedRI(self.b, self.nslices)
+
+    def nbytes(self) -> int:
+        n = self.b.numel() * 8 + self.H.numel() * 8
+        if self.prep is not None:
+            n += self.prep.buf.numel()
+        return n
+
+    def _sync_host(self, *ts):
+        with torch.cuda.stream(self.stream):
+            out = [t.to("cpu", non_blocking=False) for t in ts]
+        return [o.numpy() for o in out]
+
+    def jkh_mo(self, C):
+        self.calls["jkh_mo"] += 1
+        P = self.st.nbf5
+        with torch.cuda.stream(self.stream):
+            dC = ops.to_device(C, self.device)
+            if self.precision == "mixed":
+                res = ops.jkh_mo_ri_mixed(dC, self.H, self.prep, P)
+            else:
+                res = ops.jkh_mo_ri(dC, self.H, self.b, P)
+            return self._sync_host(*res)
+
+    def lagrange2(self, C, n, cj12, ck12):
+        self.calls["lagrange2"] += 1
+        st = self.st
+        with torch.cuda.stream(self.stream):
+            dC = ops.to_device(C, self.device)
+            dn, dcj, dck = (ops.to_device(x, self.device) for x in (n, cj12, ck12))
+            if self.precision == "mixed":
+                res = ops.lagrange2_ri_mixed(dC, self.H, self.prep, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
+            else:
+                res = ops.lagrange2_ri(dC, self.H, self.b, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
+            return self._sync_host(*res)
+
+
+@dataclasses.dataclass
+class SolveState:
+    """Optimizer settings the reference keeps on ``param`` and mutates
+    (``minimization.py:248-250``)."""
+
+    alpha: float = 0.02
+    maxloop: int = 30
+
+
+def calcorbe(y, n, cj12, ck12, C, be, p):
+    """``pnof.py:1103-1111``."""
+    Cn = C if not np.any(y) else nof.rotate_orbital(y, C, p)
+    J_MO, K_MO, H_core = be.jkh_mo(Cn)
+    return nof.calce(n, cj12, ck12, J_MO, K_MO, H_core, p)
+
+
+def calcorbg(y, n, cj12, ck12, C, be, p):
+    """``pnof.py:1114-1131``."""
+    Cn = C if not np.any(y) else nof.rotate_orbital(y, C, p)
+    np.fill_diagonal(cj12, 0.0)
+    np.fill_diagonal(ck12, 0.0)
+    elag, _ = be.lagrange2(Cn, n, cj12, ck12)
+    return nof.orbital_gradient(elag, p)
+
+
+def occoptr(gamma, C, be, p):
+    """``minimization.py:77-97``: CG over gamma at fixed orbitals."""
+    J_MO, K_MO, H_core = be.jkh_mo(C)
+    E, nit, success = 0.0, 0, True
+    if p.ndoc > 0:
+        res = scipy.optimize.minimize(nof.calcocce, gamma, args=(J_MO, K_MO, H_core, p), jac=nof.calcoccg,
+                                      method="CG")
+        gamma, E, nit, success = res.x, res.fun, res.nit, res.success
+    n, _ = nof.ocupacion_softmax(gamma, p)
+    cj12, ck12 = nof.cjckd8(n, p)
+    return E, nit, success, gamma, n, cj12, ck12
+
+
+def orbopt_adam(gamma, C, be, p, state: SolveState):
+    """``minimization.py:200-253``: AMSgrad steps of orbital rotations."""
+    n, _ = nof.ocupacion_softmax(gamma, p)
+    cj12, ck12 = nof.cjckd8(n, p)
+    y0 = np.zeros(p.nvar)
+    E = calcorbe(y0, n, cj12, ck12, C, be, p)
+    alpha, beta1, beta2 = state.alpha, 0.7, 0.999
+    m = np.zeros(p.nvar)
+    v = np.zeros(p.nvar)
+    vhat_max = np.zeros(p.nvar)
+    improved = success = False
+    best_E, best_C = E, C
+    nit = 0
+    for i in range(state.maxloop):
+        nit += 1
+        grad = calcorbg(y0, n, cj12, ck12, C, be, p)
+        if np.linalg.norm(grad) < 1e-4 and improved:
+            success = True
+            break
+        m = beta1 * m + (1 - beta1) * grad
+        v = beta2 * v + (1 - beta2) * grad ** 2
+        mhat = m / (1.0 - beta1 ** (i + 1))
+        vhat = v / (1.0 - beta2 ** (i + 1))
+        vhat_max = np.maximum(vhat_max, vhat)
+        y = -alpha * mhat / np.sqrt(vhat_max + 1e-8)
+        C = nof.rotate_orbital(y, C, p)
+        E = calcorbe(y0, n, cj12, ck12, C, be, p)
+        if E < best_E:
+            best_C, best_E = C, E
+            improved = True
+    if not improved:
+        state.alpha /= 10
+        state.maxloop += 30
+    return best_E, best_C, nit, success
+
+
+@dataclasses.dataclass
+class SolveResult:
+    E_elec: float
+    C: np.ndarray
+    gamma: np.ndarray
+    n: np.ndarray
+    iterations: int
+    converged: bool
+    history: dict
+    seconds: float
+
+
+def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_switch: float | None = None,
+          callback=None) -> SolveResult:
+    """The outer loop of ``compute_energy`` (``energy.py:112-170``).
+
+    Converged when both gradient norms are below ``tol`` (or their optimizers
+    report success), as ``energy.py:155`` (whose tolerance is 1e-3).  With
+    ``fp64_switch`` set, the backend switches from the mixed path to FP64 once
+    the orbital gradient norm falls below it."""
+    t0 = time.perf_counter()
+    p = copy.copy(p)
+    state = SolveState(alpha=getattr(p, "alpha", 0.02), maxloop=getattr(p, "maxloop", 30))
+    hist = {k: [] for k in ("E_orb", "E_occ", "g_orb", "g_occ", "nit_orb", "nit_occ", "precision")}
+    E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
+    hist["E_occ"].append(E_occ)
+    hist["nit_occ"].append(nit_occ)
+    converged = False
+    it = 0
+    for it in range(maxit):
+        E_orb, C, nit_orb, ok_orb = orbopt_adam(gamma, C, be, p, state)
+        E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
+        C, gamma = nof.order_occupations_softmax(C, gamma, p)
+        g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
+        J_MO, K_MO, H_core = be.jkh_mo(C)
+        g_occ = np.linalg.norm(nof.calcoccg(gamma, J_MO, K_MO, H_core, p))
+        for k, v in (("E_orb", E_orb), ("E_occ", E_occ), ("g_orb", g_orb), ("g_occ", g_occ), ("nit_orb", nit_orb),
+                     ("nit_occ", nit_occ), ("precision", be.precision)):
+            hist[k].append(v)
+        if callback is not None:
+            callback(it, hist)
+        if fp64_switch is not None and be.precision != "fp64" and g_orb < fp64_switch:
+            be.set_precision("fp64")
+        if (ok_orb or g_orb < tol) and (ok_occ or g_occ < tol):
+            converged = True
+            break
+    n, _ = nof.ocupacion_softmax(gamma, p)
+    cj12, ck12 = nof.cjckd8(n, p)
+    elag, Hmat = be.lagrange2(C, n, cj12, ck12)
+    P = p.nbf5
+    E = float(np.trace(elag[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat)[:P]))
+    return SolveResult(E, C, gamma, n, it + 1, converged, hist, time.perf_counter() - t0)

@@ -43,6 +43,43 @@ CASES = {
     "ragged": ("ragged", 3, False, False),
 }
 
+#: outer iterations of the reference's solve loop recorded for the loop parity test
+LOOP_CASE = ("water", 0, 3)
+
+
+def run_loop(pynof, workload, seed, n_outer):
+    """The body of compute_energy's loop (energy.py:94-153) with the
+    reference's own functions, psi4-free: occoptr, then per outer iteration
+    orbopt_adam, occoptr, order_occupations_softmax and the two gradients."""
+    st = synthetic.structure(workload)
+    b, C, H, n = synthetic.make_inputs(st, seed)
+    p = make_param(st)
+    g0 = np.log(max(0.001 / st.ncwo, 1e-16)) - np.log(0.999)
+    gamma = np.full(st.nv, g0)
+    out = dict(b=b, C0=C, H=H, gamma0=gamma.copy())
+    E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = pynof.occoptr(gamma, C, H, [], b, p)
+    rec = {"E_orb": [], "E_occ": [E_occ], "g_orb": [], "g_occ": [], "nit_orb": [], "nit_occ": [nit_occ]}
+    for it in range(n_outer):
+        E_orb, C, nit_orb, ok_orb = pynof.orbopt_adam(gamma, C, H, [], b, p)
+        E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = pynof.occoptr(gamma, C, H, [], b, p)
+        C, gamma = pynof.order_occupations_softmax(C, gamma, H, [], b, p)
+        y = np.zeros(p.nvar)
+        g_orb = pynof.calcorbg(y, n, cj12, ck12, C, H, [], b, p)
+        J_MO, K_MO, H_core = pynof.computeJKH_MO(C, H, [], b, p)
+        g_occ = pynof.calcoccg(gamma, J_MO, K_MO, H_core, p)
+        rec["E_orb"].append(E_orb)
+        rec["E_occ"].append(E_occ)
+        rec["g_orb"].append(np.linalg.norm(g_orb))
+        rec["g_occ"].append(np.linalg.norm(g_occ))
+        rec["nit_orb"].append(nit_orb)
+        rec["nit_occ"].append(nit_occ)
+        out[f"C_{it}"] = C.copy()
+        out[f"gamma_{it}"] = gamma.copy()
+    out.update({k: np.array(v) for k, v in rec.items()})
+    out["alpha_final"] = np.array(p.alpha)
+    out["maxloop_final"] = np.array(p.maxloop)
+    return out
+
 
 def import_reference(ref_src):
     sys.pycache_prefix = tempfile.mkdtemp(prefix="pycache_ref_")
@@ -198,6 +235,12 @@ def main():
         np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
         allmeta[name] = meta
         print(name, json.dumps(meta["checks"]))
+    wl, seed, n_outer = LOOP_CASE
+    loop = run_loop(pynof, wl, seed, n_outer)
+    np.savez_compressed(os.path.join(args.out, "loop_water.npz"), **loop)
+    allmeta["loop_water"] = dict(workload=wl, seed=seed, n_outer=n_outer, E_orb=loop["E_orb"].tolist(),
+                                 g_orb=loop["g_orb"].tolist(), g_occ=loop["g_occ"].tolist())
+    print("loop", allmeta["loop_water"])
     with open(os.path.join(args.out, "golden_meta.json"), "w") as f:
         json.dump(allmeta, f, indent=1, sort_keys=True)
 
