@@ -223,6 +223,27 @@ int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, co
                           const double* ck12, int nbf, int nbf5, int naux, int nbeta, int nalpha, int nslices,
                           double* elag, double* Hmat, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched A1 (many molecules of different sizes) on the tensor cores.  No
+ * counterpart in the reference, which builds one molecule per call.  The half
+ * transform, J and K GEMMs of all molecules run as three grouped launches and
+ * the whole build is captured into one CUDA graph.  tiles[0..1] choose the
+ * tile configuration of the half-transform and J phases (0: orbitals on the
+ * 128-row side; 1, 2, 3: operands swapped, orbitals on an N tile of 32, 64,
+ * 128); NULL = {0, 0}.  Inputs per molecule: C (device), the prepared factor
+ * of gb_ri_prepare_mixed; outputs J, K as for gb_jkj_ri_mixed.  The plan
+ * captures work on `stream` at creation and replays it with gb_batch_launch;
+ * the buffers must stay valid while the plan lives.
+ * ---------------------------------------------------------------------- */
+typedef struct gb_batch gb_batch;
+size_t gb_jkj_batch_workspace_mixed(int nmol, const int* nbf, const int* nbf5, const int* naux, int nslices);
+int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const void* const* prep, const int* nbf,
+                              const int* nbf5, const int* naux, int nslices, double* const* J, double* const* K,
+                              const int* tiles, void* workspace, size_t workspace_bytes, void* stream,
+                              gb_batch** plan);
+int gb_batch_launch(gb_batch* plan, void* stream);
+int gb_batch_destroy(gb_batch* plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,7 +39,9 @@ struct OutF64 {
   Index2 r, c;
 };
 
-enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2 };
+// SYM_PAIRROW (tensor-core path only): rows encode the pair i = m * pair_n + n,
+// tiles whose rows all have n < m are skipped, rows with n > m are mirrored.
+enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2, SYM_PAIRROW = 3 };
 
 struct GemmF64 {
   int M, N, K, batch;

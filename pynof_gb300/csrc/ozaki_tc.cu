@@ -1,16 +1,21 @@
 // tcgen05 split-product FP64 GEMM (see ozaki_tc.cuh).
 //
-// CTA: 18 warps.  warp 0 lane 0 is the producer: a 4-stage ring in which every
-// stage holds the S slices of a 128 x 16 block of A and of B, each operand one
-// contiguous cp.async.bulk copy (the slicer stores the digits in the
-// tensor-core core-matrix order, slice.cuh).  warp 1 allocates TMEM (512
-// columns) and its lane 0 issues tcgen05.mma (M=128, N=128, K=16,
-// bf16 -> f32).  warps 2..17 drain and finish: warp w reads TMEM lanes
-// 32 (w % 4) .. +31 (tile rows) and columns 32 ((w - 2) / 4) .. +31 of every
-// accumulator.
+// CTA tile: 128 rows of A (M) x BN rows of B (N), BN in {32, 64, 128}.
+// 18 warps.  warp 0 lane 0 is the producer: a 4-stage ring in which every
+// stage holds the S slices of a 128 x 16 block of A (one contiguous
+// cp.async.bulk copy -- the slicer stores the digits in the tensor-core
+// core-matrix order, slice.cuh) and of a BN x 16 block of B (one copy, or two
+// per slice when BN < 128).  warp 1 allocates TMEM (4 BN columns) and its
+// lane 0 issues tcgen05.mma (M=128, N=BN, K=16, bf16 -> f32).  warps 2..17
+// drain and finish: warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows) and
+// BN/4 columns from (w - 2) / 4 * BN/4 of every accumulator.
 //
-// TMEM columns: [0,128) group 2, [128,256) group 3, [256,384) group 4 (exact,
-// drained every 12 stages = 192 k), [384,512) groups 5.. (whole K).
+// TMEM columns: [0,BN) group 2, [BN,2BN) group 3, [2BN,3BN) group 4 (exact,
+// drained every 12 stages = 192 k), [3BN,4BN) groups 5.. (whole K, or per
+// chunk with fdrain).
+//
+// One launch covers one GEMM (optionally batched), or -- the grouped kernel --
+// a table of GEMMs of different shapes (e.g. one per molecule of a batch).
 //
 // Every mbarrier wait is bounded (kWaitLimitNs); on timeout the CTA records
 // GB_ERR_TIMEOUT in the device status word, stops issuing work, waits (bounded)
@@ -19,6 +24,7 @@
 
 #include <cstdio>
 #include <mutex>
+#include <vector>
 
 #include "ozaki_tc.cuh"
 
@@ -27,13 +33,23 @@ static __device__ int g_tc_status;
 namespace gb {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = SL_K, STAGES = 4, CH = 12;
+constexpr int BM = 128, BK = SL_K, STAGES = 4, CH = 12;
 constexpr int NUM_EPI_WARPS = 16, THREADS = 32 * (2 + NUM_EPI_WARPS);
 // 18 warps put 5 warps on two of the four SM sub-partitions, whose register
 // files hold 16K registers each: 5 * 32 * 96 <= 16384 caps the kernel at 96.
 constexpr int MAX_REGS = 96;
-constexpr uint32_t TILE_BYTES = SL_TILE_BYTES;  // 4 KB per slice tile (BM == BN == SL_ROWS)
-constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t TILE_BYTES = SL_TILE_BYTES;  // 4 KB per A slice tile (BM == SL_ROWS)
+
+template <int BN>
+struct TileCfg {
+  static_assert(BN == 32 || BN == 64 || BN == 128, "BN must be 32, 64 or 128");
+  static constexpr uint32_t B_TILE = BN * SL_K * 2;  // bytes of one B slice tile
+  static constexpr uint32_t TMEM_COLS = 4 * BN;      // power of two >= 32
+  static constexpr int CW = BN / 4;                  // columns per epilogue warp
+  // kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major, M=128, N=BN
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                    ((uint32_t)(BM >> 4) << 24);
+};
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
 constexpr float MAGIC = 12582912.0f;                          // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
@@ -94,26 +110,22 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-// UMMA shared-memory descriptor of one 128 x 16 slice tile: K-major, no
-// swizzle; core matrices (8 rows x 16 B) 2 KB apart along K (leading byte
-// offset) and 128 B apart along the rows (stride byte offset).
-__device__ __forceinline__ uint64_t desc_tile(uint32_t saddr) {
+// UMMA shared-memory descriptor of one slice tile of `rows` rows x 16 k:
+// K-major, no swizzle; core matrices (8 rows x 16 B) rows*16 B apart along K
+// (leading byte offset) and 128 B apart along the rows (stride byte offset).
+__device__ __forceinline__ uint64_t desc_tile(uint32_t saddr, uint32_t rows) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)(2048u >> 4) << 16;   // leading byte offset
-  d |= (uint64_t)(128u >> 4) << 32;    // stride byte offset
-  d |= (uint64_t)1 << 46;              // descriptor version
-  return d;                            // layout type 0: no swizzle
+  d |= (uint64_t)((rows * 16u) >> 4) << 16;  // leading byte offset
+  d |= (uint64_t)(128u >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  return d;                                  // layout type 0: no swizzle
 }
 
-// kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major, M=128, N=128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, bool accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(IDESC), "r"((uint32_t)accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate)
       : "memory");
 }
 
@@ -174,22 +186,24 @@ struct KArgs {
 
 // MMAs of one stage, fully unrolled for S slices: a product (s, t) reads slice
 // tile s of A and t of B, whose descriptors differ from the stage's first tile
-// descriptors only in the start-address field (+ (s - 1) * TILE_BYTES / 16).
-template <int S>
+// descriptors only in the start-address field.
+template <int S, int BN>
 __device__ __forceinline__ void issue_inexact(uint32_t tmem, uint64_t da, uint64_t db, bool& started) {
+  using T = TileCfg<BN>;
 #pragma unroll
   for (int s = 1; s <= S; ++s)
 #pragma unroll
     for (int t = 1; t <= S + 1 - s; ++t) {
       if (s + t <= 4) continue;
-      mma_bf16(tmem + 384, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)), db + (uint64_t)((t - 1) * (TILE_BYTES >> 4)),
-               started);
+      mma_bf16(tmem + 3 * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)), db + (uint64_t)((t - 1) * (T::B_TILE >> 4)),
+               T::IDESC, started);
       started = true;
     }
 }
 
-template <int S>
+template <int S, int BN>
 __device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t db, bool first) {
+  using T = TileCfg<BN>;
   constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
 #pragma unroll
   for (int gg = 2; gg <= gE; ++gg) {
@@ -197,35 +211,47 @@ __device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t
     for (int s = 1; s < gg; ++s) {
       const int t = gg - s;
       if (s > S || t > S) continue;
-      mma_bf16(tmem + (gg - 2) * 128, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)),
-               db + (uint64_t)((t - 1) * (TILE_BYTES >> 4)), !(first && s == 1));
+      mma_bf16(tmem + (gg - 2) * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)),
+               db + (uint64_t)((t - 1) * (T::B_TILE >> 4)), T::IDESC, !(first && s == 1));
     }
   }
 }
 
-template <int SLICES>
-__global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs a) {
-  extern __shared__ unsigned char smem_raw[];
-  const OzGemm& g = a.g;
-  // M tiles vary fastest, so the CTAs that share a B tile run together and the
-  // B slices are read from HBM once (L2 serves the other M tiles).
+// Local tile index -> (batch, m0, n0), M tiles fastest so that the CTAs sharing
+// a B block run together (B read once from HBM, then from L2).  Returns false
+// for tiles a symmetric output does not need.
+template <int BN>
+__device__ __forceinline__ bool decode_tile(const OzGemm& g, long long t, int& bz, int& m0, int& n0) {
   const int mtiles = (g.M + BM - 1) / BM;
-  const int m0 = (int)(blockIdx.x % mtiles) * BM;
-  const int n0 = (int)(blockIdx.x / mtiles) * BN;
-  const int bz = blockIdx.y;
-
-  if (g.sym == SYM_ROWCOL && m0 > n0) return;
+  const long long per_batch = (long long)mtiles * ((g.N + BN - 1) / BN);
+  bz = (int)(t / per_batch);
+  const long long r = t % per_batch;
+  m0 = (int)(r % mtiles) * BM;
+  n0 = (int)(r / mtiles) * BN;
+  if (g.sym == SYM_ROWCOL && m0 > n0) return false;
   if (g.sym == SYM_PAIRCOL) {
     const int j1 = min(n0 + BN, g.N) - 1;
     const int ma = n0 / g.pair_n, mb = j1 / g.pair_n;
-    if (ma == mb && (j1 % g.pair_n) < ma) return;
+    if (ma == mb && (j1 % g.pair_n) < ma) return false;
   }
-  // a CTA of this or an earlier launch gave up: do not start (the host sees the status word)
-  if (*(volatile int*)&g_tc_status != 0) return;
+  if (g.sym == SYM_PAIRROW) {
+    const int i1 = min(m0 + BM, g.M) - 1;
+    const int ma = m0 / g.pair_n, mb = i1 / g.pair_n;
+    if (ma == mb && (i1 % g.pair_n) < ma) return false;
+  }
+  return true;
+}
 
-  constexpr int S = SLICES;
+// One output tile, all roles.
+template <int S, int BN>
+__device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0, unsigned char* smem_raw) {
+  using T = TileCfg<BN>;
+  const OzGemm& g = a.g;
+  constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
+  constexpr bool has_inexact = (S + 1) > 4;
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const uint32_t stage_bytes = 2u * S * TILE_BYTES;
+  constexpr uint32_t a_bytes = (uint32_t)S * TILE_BYTES, b_bytes = (uint32_t)S * T::B_TILE;
+  constexpr uint32_t stage_bytes = a_bytes + b_bytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   // bars: full[STAGES], empty[STAGES], accfull, accempty, done
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
@@ -255,7 +281,7 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(const_cast<uint32_t*>(tmem_slot))),
-                 "r"(TMEM_COLS)
+                 "r"(T::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     tc_fence_before();
@@ -266,20 +292,18 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
 
   const int nkb = (g.K + BK - 1) / BK;
   const int nchunks = (nkb + CH - 1) / CH;
-  const int gE = min(S + 1, 4);
-  const bool has_inexact = (S + 1) > 4;
 
   if (warp == 0) {
-    // ---------------- TMA producer ----------------
+    // ---------------- producer ----------------
     if (lane == 0) {
       int issued = 0;
-      const uint32_t half = (uint32_t)S * TILE_BYTES;
       // an operand sliced once (batch 1) is shared by every batch entry
       const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
       const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
-                                (long long)(m0 / BM) * a.A.kblocks() * half;
-      const unsigned char* gb_ = reinterpret_cast<const unsigned char*>(a.B.planes) + bbz * a.B.batch_bytes() +
-                                 (long long)(n0 / BN) * a.B.kblocks() * half;
+                                (long long)(m0 / BM) * a.A.kblocks() * a_bytes;
+      const int rb = n0 / SL_ROWS, r0 = n0 % SL_ROWS;
+      const unsigned char* gbp = reinterpret_cast<const unsigned char*>(a.B.planes) + bbz * a.B.batch_bytes() +
+                                 (long long)rb * a.B.kblocks() * (S * TILE_BYTES) + (r0 / 8) * 128;
       for (int kb = 0; kb < nkb; ++kb) {
         const int st = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
@@ -289,8 +313,19 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
         }
         mbar_expect_tx(full_bar(st), stage_bytes);
         const uint32_t sa = sbase + st * stage_bytes;
-        bulk_load(sa, ga + (long long)kb * half, half, full_bar(st));
-        bulk_load(sa + half, gb_ + (long long)kb * half, half, full_bar(st));
+        bulk_load(sa, ga + (long long)kb * a_bytes, a_bytes, full_bar(st));
+        const unsigned char* gblk = gbp + (long long)kb * (S * TILE_BYTES);
+        if (BN == SL_ROWS) {
+          bulk_load(sa + a_bytes, gblk, b_bytes, full_bar(st));
+        } else {
+          // BN rows of each k group of each slice tile: two runs of BN * 16 bytes
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int kg = 0; kg < 2; ++kg)
+              bulk_load(sa + a_bytes + s * T::B_TILE + kg * (BN * 16), gblk + s * TILE_BYTES + kg * 2048, BN * 16,
+                        full_bar(st));
+        }
         ++issued;
       }
       if (*abort_flag) {
@@ -311,7 +346,7 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
         }
         tc_fence_after();
         const uint32_t sa = sbase + st * stage_bytes;
-        const uint64_t da = desc_tile(sa), db = desc_tile(sa + S * TILE_BYTES);
+        const uint64_t da = desc_tile(sa, BM), db = desc_tile(sa + a_bytes, BN);
         const int c = kb / CH;
         const bool first = (kb % CH) == 0;
         if (g.fdrain) {
@@ -324,9 +359,9 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
             tc_fence_after();
           }
           if (first) f_started = false;
-          if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
+          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, f_started);
         } else {
-          if (has_inexact) issue_inexact<S>(tmem, da, db, f_started);
+          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, f_started);
           if (first && c > 0) {
             if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
               signal_abort(abort_flag);
@@ -335,7 +370,7 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
             tc_fence_after();
           }
         }
-        issue_exact<S>(tmem, da, db, first);
+        issue_exact<S, BN>(tmem, da, db, first);
         if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(accfull_bar);
         mma_commit(empty_bar(st));
       }
@@ -343,12 +378,13 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
     }
   } else {
     // ---------------- epilogue: drain exact groups, assemble FP64 ----------------
+    constexpr int CW = T::CW;
     const int q = warp & 3;
     const int cg = (warp - 2) >> 2;
-    const uint32_t lbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * 32);
-    long long R[32];
+    const uint32_t lbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * CW);
+    long long R[CW];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) R[j] = 0;
+    for (int j = 0; j < CW; ++j) R[j] = 0;
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
       const bool got = mbar_wait(accfull_bar, c & 1, abort_flag);
@@ -363,9 +399,9 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
         const float up = __int_as_float((127 + 7 * gg) << 23);  // 2^(7 g)
         const int sh = 7 * (gE - gg) + fr;
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < CW / 8; ++h) {
           uint32_t v[8];
-          tmem_ld8(lbase + (uint32_t)((gg - 2) * 128 + h * 8), v);
+          tmem_ld8(lbase + (uint32_t)((gg - 2) * BN + h * 8), v);
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const float f = fmaf(__uint_as_float(v[j]), up, MAGIC);
@@ -377,9 +413,9 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
       if (has_inexact && g.fdrain) {
         const float upEF = __int_as_float((127 + 7 * gE + a.frac) << 23);  // 2^(7 gE + frac)
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < CW / 8; ++h) {
           uint32_t v[8];
-          tmem_ld8(lbase + 384u + (uint32_t)(h * 8), v);
+          tmem_ld8(lbase + (uint32_t)(3 * BN + h * 8), v);
 #pragma unroll
           for (int j = 0; j < 8; ++j) R[h * 8 + j] += __float2ll_rn(__uint_as_float(v[j]) * upEF);
         }
@@ -404,18 +440,23 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
       double* Cb = g.C + (long long)bz * g.c_sb;
       const long long ri = (i < g.M) ? g.c_r.at(i) : 0;
       const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
+      long long rmir = -1;  // mirrored row of a pair-symmetric row index
+      if (g.sym == SYM_PAIRROW && i < g.M) {
+        const int mm = i / g.pair_n, nn = i % g.pair_n;
+        if (nn > mm) rmir = g.c_r.at((long long)nn * g.pair_n + mm);
+      }
 #pragma unroll
-      for (int h = 0; h < 4; ++h) {
+      for (int h = 0; h < CW / 8; ++h) {
         uint32_t v[8];
         if (has_inexact && !g.fdrain) {
-          tmem_ld8(lbase + 384u + (uint32_t)(h * 8), v);
+          tmem_ld8(lbase + (uint32_t)(3 * BN + h * 8), v);
         } else {
 #pragma unroll
           for (int j = 0; j < 8; ++j) v[j] = 0u;
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const int jj = n0 + cg * 32 + h * 8 + j;
+          const int jj = n0 + cg * CW + h * 8 + j;
           if (i >= g.M || jj >= g.N) continue;
           const float t = __uint_as_float(v[j]) * upE;
           const float th = rintf(t);
@@ -425,12 +466,15 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
                                        : (long long)((unsigned long long)(R[h * 8 + j] + hi) << a.frac) + lo;
           const int eb = a.B.exps[(a.B.batch == 1 ? 0LL : (long long)bz) * g.N + jj];
           const double val = fixed_to_double(z, ea + eb - 7 * gE - a.frac, g.negate);
-          Cb[ri + g.c_c.at(jj)] = val;
+          const long long cj = g.c_c.at(jj);
+          Cb[ri + cj] = val;
           if (mirror_rc) {
             Cb[g.c_r.at(jj) + g.c_c.at(i)] = val;
           } else if (g.sym == SYM_PAIRCOL) {
             const int mm = jj / g.pair_n, nn = jj % g.pair_n;
             if (nn > mm) Cb[ri + g.c_c.at((long long)nn * g.pair_n + mm)] = val;
+          } else if (rmir >= 0) {
+            Cb[rmir + cj] = val;
           }
         }
       }
@@ -444,102 +488,207 @@ __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs
       mbar_wait(done_bar, 0, nullptr);
     }
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::TMEM_COLS) : "memory");
   }
+}
+
+template <int S, int BN>
+__global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  // a CTA of this or an earlier launch gave up: do not start (the host sees the status word)
+  if (*(volatile int*)&g_tc_status != 0) return;
+  int bz, m0, n0;
+  if (!decode_tile<BN>(a.g, (long long)blockIdx.x + (long long)blockIdx.y * gridDim.x, bz, m0, n0)) return;
+  cta_tile<S, BN>(a, bz, m0, n0, smem_raw);
+}
+
+// Grouped launch: problem p owns the tiles [starts[p], starts[p + 1]).
+template <int S, int BN>
+__global__ void __maxnreg__(MAX_REGS)
+    ozaki_grouped_kernel(const KArgs* __restrict__ probs, const long long* __restrict__ starts, int nprob) {
+  extern __shared__ unsigned char smem_raw[];
+  if (*(volatile int*)&g_tc_status != 0) return;
+  const long long t = (long long)blockIdx.x + (long long)blockIdx.y * gridDim.x;
+  int lo = 0, hi = nprob;  // find p with starts[p] <= t < starts[p + 1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (starts[mid] <= t) lo = mid; else hi = mid;
+  }
+  if (t >= starts[nprob]) return;
+  const KArgs& a = probs[lo];
+  int bz, m0, n0;
+  if (!decode_tile<BN>(a.g, t - starts[lo], bz, m0, n0)) return;
+  cta_tile<S, BN>(a, bz, m0, n0, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-size_t smem_bytes(int S) { return (size_t)STAGES * 2 * S * TILE_BYTES + 256 + 1024; }
+size_t smem_bytes(int S, int BN) { return (size_t)STAGES * S * (TILE_BYTES + BN * SL_K * 2) + 256 + 1024; }
 
 using KernelFn = void (*)(KArgs);
-KernelFn kernel_for(int S) {
+using GroupedFn = void (*)(const KArgs*, const long long*, int);
+
+template <int BN>
+KernelFn single_for(int S) {
   switch (S) {
-    case 1: return ozaki_kernel<1>;
-    case 2: return ozaki_kernel<2>;
-    case 3: return ozaki_kernel<3>;
-    case 4: return ozaki_kernel<4>;
-    case 5: return ozaki_kernel<5>;
-    default: return ozaki_kernel<6>;
+    case 1: return ozaki_kernel<1, BN>;
+    case 2: return ozaki_kernel<2, BN>;
+    case 3: return ozaki_kernel<3, BN>;
+    case 4: return ozaki_kernel<4, BN>;
+    case 5: return ozaki_kernel<5, BN>;
+    default: return ozaki_kernel<6, BN>;
   }
 }
 
-}  // namespace
+template <int BN>
+GroupedFn grouped_for(int S) {
+  switch (S) {
+    case 1: return ozaki_grouped_kernel<1, BN>;
+    case 2: return ozaki_grouped_kernel<2, BN>;
+    case 3: return ozaki_grouped_kernel<3, BN>;
+    case 4: return ozaki_grouped_kernel<4, BN>;
+    case 5: return ozaki_grouped_kernel<5, BN>;
+    default: return ozaki_grouped_kernel<6, BN>;
+  }
+}
 
-int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaStream_t stream) {
-  if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return GB_OK;
-  GB_REQUIRE(g.S >= 1 && g.S <= 6 && A.S == g.S && B.S == g.S, GB_ERR_INVALID_ARG, "ozaki_gemm: nslices mismatch");
-  GB_REQUIRE(A.rows == g.M && B.rows == g.N && A.K == g.K && B.K == g.K && (A.batch == g.batch || A.batch == 1) &&
-                 (B.batch == g.batch || B.batch == 1),
-             GB_ERR_BAD_SHAPE, "ozaki_gemm: operand shapes do not match the GEMM");
-  GB_REQUIRE(g.sym != SYM_ROWCOL || g.M == g.N, GB_ERR_BAD_SHAPE, "ozaki_gemm: SYM_ROWCOL needs M == N");
-  GB_REQUIRE(g.sym != SYM_PAIRCOL || (long long)g.pair_n * g.pair_n == g.N, GB_ERR_BAD_SHAPE,
-             "ozaki_gemm: SYM_PAIRCOL needs N == pair_n^2");
-  const long long tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
-  GB_REQUIRE(g.batch <= 65535 && tiles <= 2147483647LL, GB_ERR_BAD_SHAPE, "ozaki_gemm: grid too large");
-  if (g.K == 0) {
-    GB_REQUIRE(false, GB_ERR_BAD_SHAPE, "ozaki_gemm: K == 0");
-  }
-  GB_REQUIRE((reinterpret_cast<uintptr_t>(A.planes) & 15) == 0 && (reinterpret_cast<uintptr_t>(B.planes) & 15) == 0,
-             GB_ERR_INVALID_ARG, "ozaki_gemm: slice planes not 16-byte aligned");
-  const size_t smem = smem_bytes(g.S);
+KernelFn kernel_for(int S, int BN) {
+  return BN == 32 ? single_for<32>(S) : BN == 64 ? single_for<64>(S) : single_for<128>(S);
+}
+GroupedFn grouped_kernel_for(int S, int BN) {
+  return BN == 32 ? grouped_for<32>(S) : BN == 64 ? grouped_for<64>(S) : grouped_for<128>(S);
+}
+
+// Opt every instantiation in to its dynamic shared memory once per device.
+int configure_device() {
   static std::mutex mu;
-  static int configured_dev[64] = {0};
-  {
-    int dev = 0;
-    GB_TRY(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
-    std::lock_guard<std::mutex> lk(mu);
-    if (dev >= 0 && dev < 64 && !configured_dev[dev]) {
-      for (int sl = 1; sl <= 6; ++sl)
-        GB_TRY(cuda_status(cudaFuncSetAttribute(kernel_for(sl), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem_bytes(sl)),
-                           "cudaFuncSetAttribute"));
-      configured_dev[dev] = 1;
+  static int configured[64] = {0};
+  int dev = 0;
+  GB_TRY(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 0 || dev >= 64 || configured[dev]) return GB_OK;
+  for (int bn : {32, 64, 128})
+    for (int sl = 1; sl <= 6; ++sl) {
+      const int sm = (int)smem_bytes(sl, bn);
+      GB_TRY(cuda_status(cudaFuncSetAttribute(kernel_for(sl, bn), cudaFuncAttributeMaxDynamicSharedMemorySize, sm),
+                         "cudaFuncSetAttribute"));
+      GB_TRY(cuda_status(
+          cudaFuncSetAttribute(grouped_kernel_for(sl, bn), cudaFuncAttributeMaxDynamicSharedMemorySize, sm),
+          "cudaFuncSetAttribute"));
     }
-  }
-  // fraction bits of the fixed-point assembly: keep |z| < 2^62
-  const int nkb = (g.K + BK - 1) / BK;
+  configured[dev] = 1;
+  return GB_OK;
+}
+
+// Fraction bits of the fixed-point assembly: keep |z| < 2^62.
+int frac_bits(int S, int K) {
+  const int nkb = (K + BK - 1) / BK;
   const int nchunks = (nkb + CH - 1) / CH;
-  const int gE = g.S + 1 < 4 ? g.S + 1 : 4;
+  const int gE = S + 1 < 4 ? S + 1 : 4;
   int lg = 0;
   while ((1 << lg) < nchunks) ++lg;
   const int rbits = lg + 22 + 7 * (gE - 2) + 2;
   int frac = 62 - rbits;
   if (frac > 16) frac = 16;
   if (frac < 0) frac = 0;
-  KArgs ka{g, A, B, frac};
-  if (g.K > 4096) ka.g.fdrain = 1;
-  dim3 grid((unsigned)tiles, (unsigned)g.batch);
-  const int pi = prof_begin(g.tag, stream);
-  kernel_for(g.S)<<<grid, THREADS, smem, stream>>>(ka);
-  prof_end(pi, stream);
-  const cudaError_t le = cudaGetLastError();
-  if (le != cudaSuccess) {
-    char info[512];
-    ozaki_kernel_info(info, sizeof(info));
-    set_error(GB_ERR_CUDA, "%s: %s (threads %d, dynamic smem %zu; %s)", g.tag, cudaGetErrorString(le), THREADS,
-              smem, info);
-    return GB_ERR_CUDA;
-  }
+  return frac;
+}
+
+int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
+  GB_REQUIRE(g.S >= 1 && g.S <= 6 && A.S == g.S && B.S == g.S, GB_ERR_INVALID_ARG, "ozaki_gemm: nslices mismatch");
+  GB_REQUIRE(g.bn == 32 || g.bn == 64 || g.bn == 128, GB_ERR_INVALID_ARG, "ozaki_gemm: N tile %d not in {32,64,128}",
+             g.bn);
+  GB_REQUIRE(A.rows == g.M && B.rows == g.N && A.K == g.K && B.K == g.K && (A.batch == g.batch || A.batch == 1) &&
+                 (B.batch == g.batch || B.batch == 1),
+             GB_ERR_BAD_SHAPE, "ozaki_gemm: operand shapes do not match the GEMM");
+  GB_REQUIRE(g.sym != SYM_ROWCOL || (g.M == g.N && g.bn == BM), GB_ERR_BAD_SHAPE,
+             "ozaki_gemm: SYM_ROWCOL needs M == N and 128-wide tiles");
+  GB_REQUIRE(g.sym != SYM_PAIRCOL || (long long)g.pair_n * g.pair_n == g.N, GB_ERR_BAD_SHAPE,
+             "ozaki_gemm: SYM_PAIRCOL needs N == pair_n^2");
+  GB_REQUIRE(g.sym != SYM_PAIRROW || (long long)g.pair_n * g.pair_n == g.M, GB_ERR_BAD_SHAPE,
+             "ozaki_gemm: SYM_PAIRROW needs M == pair_n^2");
+  GB_REQUIRE(g.K > 0 && g.batch <= 65535, GB_ERR_BAD_SHAPE, "ozaki_gemm: bad K or batch");
+  GB_REQUIRE((reinterpret_cast<uintptr_t>(A.planes) & 15) == 0 && (reinterpret_cast<uintptr_t>(B.planes) & 15) == 0,
+             GB_ERR_INVALID_ARG, "ozaki_gemm: slice planes not 16-byte aligned");
   return GB_OK;
 }
 
-int ozaki_kernel_info(char* out, size_t len) {
-  cudaFuncAttributes fa{};
-  cudaError_t e = cudaFuncGetAttributes(&fa, kernel_for(6));
-  int occ = -1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(6), THREADS, smem_bytes(6));
-  int dev = 0, regs_sm = 0, smem_optin = 0, max_thr = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  cudaDeviceGetAttribute(&max_thr, cudaDevAttrMaxThreadsPerBlock, dev);
-  snprintf(out, len,
-           "attr=%s regs=%d maxThreadsPerBlock=%d localBytes=%zu staticSmem=%zu maxDynSmem=%d occupancy=%d "
-           "regsPerSM=%d smemOptin=%d devMaxThreads=%d",
-           cudaGetErrorString(e), fa.numRegs, fa.maxThreadsPerBlock, fa.localSizeBytes, fa.sharedSizeBytes,
-           fa.maxDynamicSharedSizeBytes, occ, regs_sm, smem_optin, max_thr);
+KArgs make_args(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
+  KArgs ka{g, A, B, frac_bits(g.S, g.K)};
+  if (g.K > 4096) ka.g.fdrain = 1;
+  return ka;
+}
+
+dim3 grid_for(long long tiles) {
+  // x up to 2^31 - 1; split very large tile counts over y
+  const long long gx = tiles < 2147483647LL ? tiles : 65536;
+  return dim3((unsigned)gx, (unsigned)((tiles + gx - 1) / gx));
+}
+
+int launch_error(const char* tag, cudaError_t le, int S, int BN) {
+  char info[512];
+  ozaki_kernel_info(info, sizeof(info));
+  set_error(GB_ERR_CUDA, "%s: %s (S=%d BN=%d threads %d, dynamic smem %zu; %s)", tag, cudaGetErrorString(le), S, BN,
+            THREADS, smem_bytes(S, BN), info);
+  return GB_ERR_CUDA;
+}
+
+}  // namespace
+
+long long ozaki_tiles(const OzGemm& g) {
+  return ((long long)(g.M + BM - 1) / BM) * ((g.N + g.bn - 1) / g.bn) * (long long)g.batch;
+}
+
+int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaStream_t stream) {
+  if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return GB_OK;
+  GB_TRY(check_problem(A, B, g));
+  GB_TRY(configure_device());
+  const KArgs ka = make_args(A, B, g);
+  const long long tiles = ozaki_tiles(g);
+  const int pi = prof_begin(g.tag, stream);
+  kernel_for(g.S, g.bn)<<<grid_for(tiles), THREADS, smem_bytes(g.S, g.bn), stream>>>(ka);
+  prof_end(pi, stream);
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) return launch_error(g.tag, le, g.S, g.bn);
+  return GB_OK;
+}
+
+size_t ozaki_group_table_bytes(int nprob) {
+  return align256((size_t)nprob * sizeof(KArgs)) + align256((size_t)(nprob + 1) * sizeof(long long));
+}
+
+int ozaki_group_upload(const OzProblem* probs, int nprob, void* table) {
+  GB_REQUIRE(nprob >= 1 && probs && table, GB_ERR_INVALID_ARG, "ozaki_group_upload: empty group");
+  std::vector<KArgs> args;
+  std::vector<long long> starts(1, 0);
+  for (int i = 0; i < nprob; ++i) {
+    GB_TRY(check_problem(probs[i].A, probs[i].B, probs[i].g));
+    GB_REQUIRE(probs[i].g.S == probs[0].g.S && probs[i].g.bn == probs[0].g.bn, GB_ERR_INVALID_ARG,
+               "ozaki_group_upload: a group shares one slice count and tile width");
+    args.push_back(make_args(probs[i].A, probs[i].B, probs[i].g));
+    starts.push_back(starts.back() + ozaki_tiles(probs[i].g));
+  }
+  char* t = static_cast<char*>(table);
+  GB_TRY(cuda_status(cudaMemcpy(t, args.data(), nprob * sizeof(KArgs), cudaMemcpyHostToDevice), "group table"));
+  GB_TRY(cuda_status(cudaMemcpy(t + align256((size_t)nprob * sizeof(KArgs)), starts.data(),
+                                (nprob + 1) * sizeof(long long), cudaMemcpyHostToDevice),
+                     "group table"));
+  return GB_OK;
+}
+
+int ozaki_gemm_grouped(const void* table, int nprob, long long total_tiles, int S, int bn, cudaStream_t stream,
+                       const char* tag) {
+  if (total_tiles <= 0) return GB_OK;
+  GB_TRY(configure_device());
+  const char* t = static_cast<const char*>(table);
+  const KArgs* probs = reinterpret_cast<const KArgs*>(t);
+  const long long* starts = reinterpret_cast<const long long*>(t + align256((size_t)nprob * sizeof(KArgs)));
+  const int pi = prof_begin(tag, stream);
+  grouped_kernel_for(S, bn)<<<grid_for(total_tiles), THREADS, smem_bytes(S, bn), stream>>>(probs, starts, nprob);
+  prof_end(pi, stream);
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) return launch_error(tag, le, S, bn);
   return GB_OK;
 }
 
@@ -551,6 +700,24 @@ int ozaki_status(int reset, int* out) {
     GB_TRY(cuda_status(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(int)), "reset tensor-core status"));
   }
   *out = v;
+  return GB_OK;
+}
+
+int ozaki_kernel_info(char* out, size_t len) {
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel_for(6, 128));
+  int occ = -1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(6, 128), THREADS, smem_bytes(6, 128));
+  int dev = 0, regs_sm = 0, smem_optin = 0, max_thr = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&max_thr, cudaDevAttrMaxThreadsPerBlock, dev);
+  snprintf(out, len,
+           "attr=%s regs=%d maxThreadsPerBlock=%d localBytes=%zu staticSmem=%zu maxDynSmem=%d occupancy=%d "
+           "regsPerSM=%d smemOptin=%d devMaxThreads=%d",
+           cudaGetErrorString(e), fa.numRegs, fa.maxThreadsPerBlock, fa.localSizeBytes, fa.sharedSizeBytes,
+           fa.maxDynamicSharedSizeBytes, occ, regs_sm, smem_optin, max_thr);
   return GB_OK;
 }
 

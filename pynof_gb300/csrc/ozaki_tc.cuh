@@ -35,11 +35,29 @@ struct OzGemm {
   // error then stops growing with K.  Costs the overlap of the drain with
   // the MMAs; used for long contractions (K > 4096).
   int fdrain = 0;
+  int bn = 128;  // N tile width: 32, 64 or 128 (128 required for SYM_ROWCOL)
   const char* tag = "ozaki_tc";
+};
+
+// One GEMM of a grouped launch.
+struct OzProblem {
+  SlicedDesc A, B;
+  OzGemm g;
 };
 
 // A: rows are the M index; B: rows are the N index; both K-major slices.
 int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaStream_t stream);
+
+// Several GEMMs (same slice count and N tile width) in one launch.  `table`
+// is caller device memory of ozaki_group_table_bytes(n) bytes; it is filled
+// here with a synchronous copy, so a grouped launch can be captured into a
+// CUDA graph once the table holds the problem list.
+size_t ozaki_group_table_bytes(int nprob);
+int ozaki_group_upload(const OzProblem* probs, int nprob, void* table);
+int ozaki_gemm_grouped(const void* table, int nprob, long long total_tiles, int S, int bn, cudaStream_t stream,
+                       const char* tag);
+// Tiles of one problem (for building the grouped tile ranges).
+long long ozaki_tiles(const OzGemm& g);
 
 // Device status word of the tensor-core kernels (0 = ok, GB_ERR_TIMEOUT when a
 // bounded wait gave up).  Reading synchronises the current device.

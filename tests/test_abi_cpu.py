@@ -54,3 +54,22 @@ def test_workspace_queries(lib):
 def test_version_and_error(lib):
     assert lib.gb_version() >= 100
     assert isinstance(lib.gb_last_error(), bytes)
+
+
+def declared_arity():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(gb_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header(lib):
+    from pynof_gb300 import _lib
+
+    arity = declared_arity()
+    for name, (_, args) in _lib.SIGNATURES.items():
+        assert name in arity, name
+        assert len(args) == arity[name], f"{name}: ctypes has {len(args)} arguments, header {arity[name]}"
