@@ -57,6 +57,15 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
+    ap.add_argument("--mode", choices=["jk", "batch", "serve"], default="jk",
+                    help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream")
+    ap.add_argument("--nmol", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=16)
+    ap.add_argument("--rate", type=float, default=10.0)
+    ap.add_argument("--nbf-max", type=int, default=150)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--tol", type=float, default=1e-5)
+    ap.add_argument("--maxit", type=int, default=200)
     return ap.parse_args()
 
 
@@ -409,10 +418,106 @@ def measure_dgemm_tflops(torch, dev, n=8192, reps=3):
     return 2.0 * n ** 3 / best / 1e12
 
 
+def run_batch(args):
+    """64 molecules, nbf log-uniform in [24, 400], naux = 4 nbf, nbf5 ~ nbf/2:
+    one batched build (grouped launches in a CUDA graph, autotuned tiles)
+    against 64 sequential single-molecule builds (FP64 and mixed)."""
+    import torch
+
+    from pynof_gb300 import batch as bmod
+    from pynof_gb300 import ops, synthetic
+
+    torch.cuda.set_device(0)
+    sizes = synthetic.batch_sizes(args.nmol)
+    mols, fp64_in = [], []
+    for i, nbf in enumerate(sizes):
+        st = synthetic.Structure.for_nbf(nbf)
+        b, C, H, n = synthetic.make_inputs(st, 1000 + i)
+        db, dC = ops.to_device(b), ops.to_device(C)
+        mols.append((dC, ops.PreparedRI(db, args.nslices), st.nbf5))
+        fp64_in.append((dC, db, st.nbf5))
+    torch.cuda.synchronize()
+    flops = sum(flops_jkj(m[1].nbf, m[2], m[1].naux) for m in mols)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    t64 = timed(lambda: [ops.jkj_ri(c, bb, p) for c, bb, p in fp64_in], 1)
+    tmx = timed(lambda: [ops.jkj_ri_mixed(c, pr, p) for c, pr, p in mols], args.steps)
+    tiles, info = bmod.autotune(mols, reps=2, use_cache=False)
+    plan = bmod.BatchJK(mols, tiles=tiles)
+    stream = plan.stream
+    plan.run()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run()
+    e1.record(stream)
+    e1.synchronize()
+    tgr = e0.elapsed_time(e1) / 1e3 / args.steps
+    ops.check_device_status()
+    # accuracy of the batched build against the FP64 builds
+    err = 0.0
+    for (c, bb, p), J, K in zip(fp64_in, plan.J, plan.K):
+        J64, K64 = ops.jkj_ri(c, bb, p)
+        err = max(err, float((J - J64).abs().max() / J64.abs().max()), float((K - K64).abs().max() / K64.abs().max()))
+    nm = len(mols)
+    line = {"metric": "batched RI-JK builds/s, 64 molecules nbf log-uniform in [24,400]", "unit": "builds/s",
+            "value": nm / tgr, "steps": args.steps, "dtype": "bf16-split-f64", "data": "synthetic",
+            "config": {"workload": f"{nm} molecules, nbf {min(sizes)}..{max(sizes)} (median "
+                                   f"{int(np.median(sizes))}), naux=4 nbf, nbf5=5 (nbf//10)",
+                       "nslices": args.nslices, "tiles": list(tiles), "autotune": info.get("timings")},
+            "grouped_graph_s": tgr, "sequential_mixed_s": tmx, "sequential_fp64_s": t64,
+            "speedup_vs_sequential_mixed": tmx / tgr, "speedup_vs_sequential_fp64": t64 / tgr,
+            "fp64_equivalent_tflops": flops / tgr / 1e12, "max_normwise_err_vs_fp64": err}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """A Poisson stream of full NOF solves, continuous batching, mixed path
+    (switching to FP64 near convergence) against the plain FP64 path."""
+    import torch
+
+    from pynof_gb300 import serve
+
+    torch.cuda.set_device(0)
+    reqs = serve.poisson_stream(args.requests, args.rate, 24, args.nbf_max, seed=11)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        srv = serve.Server(hbm_budget=150e9, slots=args.slots, precision=prec, nslices=args.nslices,
+                           fp64_switch=1e-2, tol=args.tol, maxit=args.maxit)
+        out[prec] = srv.run(reqs)
+        out[prec]["energies"] = {r.rid: r.E_elec for r in srv.results}
+    dE = max((abs(out["mixed"]["energies"][k] - v) for k, v in out["fp64"]["energies"].items()
+              if k in out["mixed"]["energies"]), default=float("nan"))
+    for prec in out:
+        out[prec].pop("energies")
+    line = {"metric": "served NOF solves: p50/p99 latency and solves/s", "unit": "solves/s",
+            "value": out["mixed"]["solves_per_s"], "data": "synthetic",
+            "config": {"requests": args.requests, "rate_per_s": args.rate, "nbf": f"log-uniform 24..{args.nbf_max}",
+                       "naux": "4 nbf", "tol": args.tol, "maxit": args.maxit, "slots": args.slots,
+                       "hbm_budget_gb": 150, "fp64_switch_grad": 1e-2},
+            "mixed": out["mixed"], "plain_fp64": out["fp64"], "max_abs_dE_mixed_vs_fp64_hartree": dE}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "batch":
+        run_batch(args)
+    elif args.mode == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 
