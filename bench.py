@@ -496,9 +496,9 @@ def run_serve(args):
         srv = serve.Server(hbm_budget=150e9, slots=args.slots, precision=prec, nslices=args.nslices,
                            fp64_switch=1e-2, tol=args.tol, maxit=args.maxit)
         out[prec] = srv.run(reqs)
-        out[prec]["energies"] = {r.rid: r.E_elec for r in srv.results}
-    dE = max((abs(out["mixed"]["energies"][k] - v) for k, v in out["fp64"]["energies"].items()
-              if k in out["mixed"]["energies"]), default=float("nan"))
+        out[prec]["energies"] = {r.rid: r.E_elec for r in srv.results if r.converged}
+    both = [k for k in out["fp64"]["energies"] if k in out["mixed"]["energies"]]
+    dE = max((abs(out["mixed"]["energies"][k] - out["fp64"]["energies"][k]) for k in both), default=float("nan"))
     for prec in out:
         out[prec].pop("energies")
     line = {"metric": "served NOF solves: p50/p99 latency and solves/s", "unit": "solves/s",
@@ -506,7 +506,8 @@ def run_serve(args):
             "config": {"requests": args.requests, "rate_per_s": args.rate, "nbf": f"log-uniform 24..{args.nbf_max}",
                        "naux": "4 nbf", "tol": args.tol, "maxit": args.maxit, "slots": args.slots,
                        "hbm_budget_gb": 150, "fp64_switch_grad": 1e-2},
-            "mixed": out["mixed"], "plain_fp64": out["fp64"], "max_abs_dE_mixed_vs_fp64_hartree": dE}
+            "mixed": out["mixed"], "plain_fp64": out["fp64"],
+            "max_abs_dE_mixed_vs_fp64_hartree": dE, "dE_over_requests_converged_in_both": len(both)}
     print(json.dumps(line), flush=True)
 
 
