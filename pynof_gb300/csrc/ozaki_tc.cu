@@ -98,6 +98,19 @@ __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_fla
   }
 }
 
+// Named barrier of the 16 epilogue warps with an OR reduction: every one of
+// them gets the same answer, so their control flow cannot diverge.
+__device__ __forceinline__ bool epi_barrier_any(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pin, pout;\n setp.ne.u32 pin, %1, 0;\n"
+      " bar.red.or.pred pout, 1, %2, pin;\n selp.u32 %0, 1, 0, pout;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "n"(NUM_EPI_WARPS * 32)
+      : "memory");
+  return r != 0;
+}
+
 __device__ __forceinline__ void signal_abort(volatile int* abort_flag) {
   *abort_flag = 1;
   atomicExch(&g_tc_status, GB_ERR_TIMEOUT);
@@ -252,7 +265,10 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr uint32_t a_bytes = (uint32_t)S * TILE_BYTES, b_bytes = (uint32_t)S * T::B_TILE;
   constexpr uint32_t stage_bytes = a_bytes + b_bytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+  // the assembly parks the tile's int64 results in the stage buffers
+  constexpr uint32_t zs_bytes = BM * (BN + 1) * 8;
+  constexpr uint32_t data_bytes = STAGES * stage_bytes > zs_bytes ? STAGES * stage_bytes : zs_bytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + data_bytes);
   // bars: full[STAGES], empty[STAGES], accfull, accempty, done
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
@@ -426,25 +442,18 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
     }
     if (ok) {
       const bool got = mbar_wait(done_bar, 0, abort_flag);
-      if (!__all_sync(0xffffffffu, got)) {
-        signal_abort(abort_flag);
-        ok = false;
-      }
+      if (!__all_sync(0xffffffffu, got)) signal_abort(abort_flag);
     }
+    // CTA-uniform go / no-go for the assembly (every epilogue warp arrives here)
+    if (epi_barrier_any(*abort_flag != 0)) ok = false;
     if (ok) {
       tc_fence_after();
-      const int i = m0 + q * 32 + lane;
+      // 1) fold the FP32 accumulator into the fixed point and park z in shared
+      //    memory (the stage buffers are idle once every MMA has completed)
+      const int row = q * 32 + lane;
       const float upE = __int_as_float((127 + 7 * gE) << 23);
       const float upF = __int_as_float((127 + a.frac) << 23);
-      const int ea = (i < g.M) ? a.A.exps[(a.A.batch == 1 ? 0LL : (long long)bz) * g.M + i] : 0;
-      double* Cb = g.C + (long long)bz * g.c_sb;
-      const long long ri = (i < g.M) ? g.c_r.at(i) : 0;
-      const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
-      long long rmir = -1;  // mirrored row of a pair-symmetric row index
-      if (g.sym == SYM_PAIRROW && i < g.M) {
-        const int mm = i / g.pair_n, nn = i % g.pair_n;
-        if (nn > mm) rmir = g.c_r.at((long long)nn * g.pair_n + mm);
-      }
+      long long* Zs = reinterpret_cast<long long*>(smem);
 #pragma unroll
       for (int h = 0; h < CW / 8; ++h) {
         uint32_t v[8];
@@ -456,26 +465,40 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          const int jj = n0 + cg * CW + h * 8 + j;
-          if (i >= g.M || jj >= g.N) continue;
-          const float t = __uint_as_float(v[j]) * upE;
-          const float th = rintf(t);
-          const long long hi = __float2ll_rn(th);
-          const long long lo = __float2ll_rn((t - th) * upF);
-          const long long z = g.fdrain ? R[h * 8 + j]
-                                       : (long long)((unsigned long long)(R[h * 8 + j] + hi) << a.frac) + lo;
-          const int eb = a.B.exps[(a.B.batch == 1 ? 0LL : (long long)bz) * g.N + jj];
-          const double val = fixed_to_double(z, ea + eb - 7 * gE - a.frac, g.negate);
-          const long long cj = g.c_c.at(jj);
-          Cb[ri + cj] = val;
-          if (mirror_rc) {
-            Cb[g.c_r.at(jj) + g.c_c.at(i)] = val;
-          } else if (g.sym == SYM_PAIRCOL) {
-            const int mm = jj / g.pair_n, nn = jj % g.pair_n;
-            if (nn > mm) Cb[ri + g.c_c.at((long long)nn * g.pair_n + mm)] = val;
-          } else if (rmir >= 0) {
-            Cb[rmir + cj] = val;
+          long long z = R[h * 8 + j];
+          if (!g.fdrain) {
+            const float t = __uint_as_float(v[j]) * upE;
+            const float th = rintf(t);
+            z = (long long)((unsigned long long)(z + __float2ll_rn(th)) << a.frac) + __float2ll_rn((t - th) * upF);
           }
+          Zs[row * (BN + 1) + cg * CW + h * 8 + j] = z;
+        }
+      }
+      epi_barrier_any(false);
+      // 2) assemble FP64 and store, consecutive lanes on the unit-stride index
+      const int ew = warp - 2;  // 0..15
+      double* Cb = g.C + (long long)bz * g.c_sb;
+      const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
+      const int* ea_p = a.A.exps + abz * g.M;
+      const int* eb_p = a.B.exps + bbz * g.N;
+      const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
+      const bool rows_fast = g.c_c.div == 0 && g.c_c.s0 == 1 ? false : (g.c_r.div == 0 && g.c_r.s0 == 1);
+      for (int e = ew * 32 + lane; e < BM * BN; e += NUM_EPI_WARPS * 32) {
+        // element e -> (r, c): lanes along c (row-major outputs) or along r
+        const int r = rows_fast ? (e % BM) : (e / BN);
+        const int c = rows_fast ? (e / BM) : (e % BN);
+        const int i = m0 + r, jj = n0 + c;
+        if (i >= g.M || jj >= g.N) continue;
+        const double val = fixed_to_double(Zs[r * (BN + 1) + c], ea_p[i] + eb_p[jj] - 7 * gE - a.frac, g.negate);
+        Cb[g.c_r.at(i) + g.c_c.at(jj)] = val;
+        if (mirror_rc) {
+          Cb[g.c_r.at(jj) + g.c_c.at(i)] = val;
+        } else if (g.sym == SYM_PAIRCOL) {
+          const int mm = jj / g.pair_n, nn = jj % g.pair_n;
+          if (nn > mm) Cb[g.c_r.at(i) + g.c_c.at((long long)nn * g.pair_n + mm)] = val;
+        } else if (g.sym == SYM_PAIRROW) {
+          const int mm = i / g.pair_n, nn = i % g.pair_n;  // mirrored row of a pair-symmetric row
+          if (nn > mm) Cb[g.c_r.at((long long)nn * g.pair_n + mm) + g.c_c.at(jj)] = val;
         }
       }
     }
@@ -524,7 +547,11 @@ __global__ void __maxnreg__(MAX_REGS)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-size_t smem_bytes(int S, int BN) { return (size_t)STAGES * S * (TILE_BYTES + BN * SL_K * 2) + 256 + 1024; }
+size_t smem_bytes(int S, int BN) {
+  const size_t stages = (size_t)STAGES * S * (TILE_BYTES + BN * SL_K * 2);
+  const size_t zs = (size_t)BM * (BN + 1) * 8;
+  return (stages > zs ? stages : zs) + 256 + 1024;
+}
 
 using KernelFn = void (*)(KArgs);
 using GroupedFn = void (*)(const KArgs*, const long long*, int);
