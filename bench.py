@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
-    ap.add_argument("--mode", choices=["jk", "batch", "serve"], default="jk",
-                    help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream")
+    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision"], default="jk",
+                    help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream; "
+                         "precision: every split form against FP64 (J, K, E, orbital gradient)")
     ap.add_argument("--nmol", type=int, default=64)
     ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rate", type=float, default=10.0)
@@ -226,17 +227,15 @@ def run_reference(args):
 
 def run_ours(args):
     import torch
-    import torch.distributed as dist
 
     from pynof_gb300 import _lib, integrals, ops
+    from pynof_gb300.replicas import Replicas
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    reps = Replicas(device=dev)
+    world, rank = reps.world, reps.rank
 
     st, b, C, H, n = make_workload(args.workload)
     N, P, Q = st.nbf, st.nbf5, st.nbfaux
@@ -245,18 +244,7 @@ def run_ours(args):
     ops.check_device_status()
     asym = ops.check_symmetric(db)
     assert asym == 0.0, asym
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier = reps.barrier
 
     mixed = args.precision == "mixed"
     S = args.nslices
@@ -302,8 +290,7 @@ def run_ours(args):
     clk = clocks.stop()
     if mixed:
         ops.check_device_status()
-    dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3)
-    value = world * args.steps / dev_s
+    value, dev_s = reps.throughput(args.steps, e0.elapsed_time(e1) / 1e3)
 
     # ---- end-to-end leg through the drop-in call -------------------------
     C_pin = torch.from_numpy(C).pin_memory().numpy()
@@ -316,8 +303,7 @@ def run_ours(args):
     for _ in range(args.steps):
         Jh, Kh = integrals.JKj_RI_GPU(C_pin, db, p)
     barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = world * args.steps / e2e_s
+    e2e_value, e2e_s = reps.throughput(args.steps, time.perf_counter() - t0)
     h2d = C.nbytes
     d2h = 2 * P * N * N * 8
     del Jh, Kh
@@ -333,7 +319,7 @@ def run_ours(args):
             J64, K64 = ops.jkj_ri(dC, db, P)
         f1.record(stream)
         barrier()
-        fp64_s = max_over_ranks(f0.elapsed_time(f1) / 1e3)
+        fp64_s = reps.max(f0.elapsed_time(f1) / 1e3)
         dH = ops.to_device(H)
         dn = ops.to_device(n)
         cj = 2.0 * torch.outer(dn, dn)
@@ -358,12 +344,23 @@ def run_ours(args):
     name, (launches, total_ms) = top
     per_launch_s = total_ms / 1e3 / launches
     fl = KERNEL_FLOPS.get(name, lambda N, P, Q: float("nan"))(N, P, Q)
+    traffic = None
+    if name == "ozaki_tc:half_transform" and S <= 6:
+        # DRAM bytes per launch: an ncu capture of this kernel at nbf=300 read +
+        # wrote 1.727 GB for 1.728 GB of algorithmic bytes (b's digit planes
+        # once + T written); the same ratio applied to this workload's bytes
+        kpad = -(-N // 16) * 16
+        alg_bytes = float(N) * Q * kpad * 2 * S + 8.0 * P * N * Q
+        traffic = 0.9994 * alg_bytes
     if name.startswith("ozaki_tc"):
         tensor_fl = n_products(S) * fl
         achieved = tensor_fl / per_launch_s / 1e12
         peak = float(peaks["bf16_tflops"])
         roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_note": None if traffic is None else (
+                    "bytes per launch, scaled from dram__bytes_read.sum + dram__bytes_write.sum of the same kernel "
+                    f"at nbf=300 (ncu) by the algorithmic bytes ({alg_bytes:.4g} here)"),
                 "peak_source": f"bf16_tflops of {peak_src} MEASURED_PEAKS.json (burst; kernel timed alone)",
                 "achieved_definition": f"{n_products(S)} bf16 slice products x reference-formulation flops "
                                        "of the launch / launch time",
@@ -398,8 +395,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(b, C, P, sample, N, Q)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def measure_dgemm_tflops(torch, dev, n=8192, reps=3):
@@ -511,6 +507,107 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """Each arithmetic form of the path on the same seeded inputs: JK builds/s
+    (computeJKj) and computeLagrange2 calls/s, with the errors of J, K, the
+    energy E = tr elag[:P,:P] + sum_i n_i Hmat_ii and the packed orbital
+    gradient 4 (elag - elag^T) against the FP64 (DMMA) path."""
+    import torch
+
+    from pynof_gb300 import nof, ops
+
+    torch.cuda.set_device(0)
+    st, b, C, H, n = make_workload(args.workload)
+    N, P, Q = st.nbf, st.nbf5, st.nbfaux
+    db, dC, dH, dn = (ops.to_device(x) for x in (b, C, H, n))
+    cj, ck = nof.cjckd8(n, st)
+    np.fill_diagonal(cj, 0.0)
+    np.fill_diagonal(ck, 0.0)
+    dcj, dck = ops.to_device(cj), ops.to_device(ck)
+    iu, ju = np.triu_indices(N, 1)
+    keep = iu < P
+
+    def timed(fn, reps):
+        out = fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1) / 1e3 / reps
+
+    def energy_grad(elag, Hmat):
+        el = elag.cpu().numpy()
+        E = float(np.trace(el[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat.cpu().numpy())[:P]))
+        g = 4.0 * (el - el.T)
+        return E, g[iu[keep], ju[keep]]
+
+    def nrel(a, r):
+        return float((a - r).abs().max() / r.abs().max())
+
+    forms = [("fp64", None), ("mixed_s6", 6), ("bf16x3", 2), ("tf32x3", ops.SPLIT_TF32X3)]
+    out, ref = {}, None
+    for name, code in forms:
+        if code is None:
+            (J, K), t_jk = timed(lambda: ops.jkj_ri(dC, db, P), 1)
+            (JM, KM, Hc), t_mo = timed(lambda: ops.jkh_mo_ri(dC, dH, db, P), 1)
+            (el, Hm), t_l2 = timed(lambda: ops.lagrange2_ri(dC, dH, db, dn, dcj, dck, P, st.nbeta, st.nalpha), 1)
+        else:
+            prep = ops.PreparedRI(db, code)
+            (J, K), t_jk = timed(lambda: ops.jkj_ri_mixed(dC, prep, P), args.steps)
+            (JM, KM, Hc), t_mo = timed(lambda: ops.jkh_mo_ri_mixed(dC, dH, prep, P), args.steps)
+            (el, Hm), t_l2 = timed(lambda: ops.lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta,
+                                                                 st.nalpha), args.steps)
+            ops.check_device_status()
+            del prep
+        E, g = energy_grad(el, Hm)
+        rec = {"jk_builds_per_s": 1.0 / t_jk, "jkh_mo_per_s": 1.0 / t_mo, "lagrange2_per_s": 1.0 / t_l2,
+               "E_hartree": E}
+        if ref is None:
+            ref = (J, K, JM, KM, E, g)
+        else:
+            J64, K64, JM64, KM64, E64, g64 = ref
+            rec.update({
+                "J_normwise_err": nrel(J, J64), "K_normwise_err": nrel(K, K64),
+                "J_MO_normwise_err": nrel(JM, JM64), "K_MO_normwise_err": nrel(KM, KM64),
+                "E_abs_err_hartree": abs(E - E64),
+                "grad_normwise_err": float(np.abs(g - g64).max() / np.abs(g64).max()),
+                "grad_max_abs_err": float(np.abs(g - g64).max()),
+            })
+        out[name] = rec
+        del J, K, JM, KM, Hc, el, Hm
+        torch.cuda.empty_cache()
+    # the reference algorithm on the host cores (numpy / OpenBLAS restatement)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import pynof_oracle as orc
+
+        sample = max(2, P // 5)
+        orc.jkj_ri(C, b, 2)
+        t0 = time.perf_counter()
+        orc.jkj_ri(C, b, sample)
+        t_a1 = (time.perf_counter() - t0) * P / sample
+        t0 = time.perf_counter()
+        orc.jkh_mo_ri(C, H, b, P)
+        t_a3 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st)
+        t_a5 = time.perf_counter() - t0
+        cpu = {"cores": os.cpu_count(), "kind": "port",
+               "sample": f"computeJKj on {sample} of {P} orbitals (scaled), computeJKH_MO and computeLagrange2 "
+                         "whole, one call each",
+               "jk_builds_per_s": 1.0 / t_a1, "jkh_mo_per_s": 1.0 / t_a3, "lagrange2_per_s": 1.0 / t_a5}
+    line = {"metric": "precision forms of the RI JK build and Lagrangian vs FP64", "unit": "builds/s",
+            "value": out["mixed_s6"]["jk_builds_per_s"], "data": "synthetic",
+            "config": {"workload": f"nbf={N} naux={Q} nbf5={P}", "steps": args.steps,
+                       "coefficients": "GNOF (PNOF8) cj12, ck12 from the synthetic occupations",
+                       "reference": "FP64 DMMA path (parity-tested against the oracle at 1e-10)"},
+            "forms": out, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -519,6 +616,8 @@ def main():
         run_batch(args)
     elif args.mode == "serve":
         run_serve(args)
+    elif args.mode == "precision":
+        run_precision(args)
     else:
         run_ours(args)
 

@@ -171,6 +171,18 @@ int gb_energy_elec_f64(const double* elag, const double* C, const double* H, con
                        int nbeta, int nalpha, int high_spin, double* E, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* Orbital rotation C' = C expm(Y) in FP64 on the device.  Replaces
+ * rotate_orbital (utils.py:550-565), which builds Y on the host and calls
+ * scipy.linalg.expm.  y: the packed step, nvar = nbf (nbf - 1) / 2 -
+ * (nbf - nbf5) (nbf - nbf5 - 1) / 2 values over (i < nbf5, j > i) in row-major
+ * order (Y[i][j] = y, Y[j][i] = -y); C, Cout: [nbf][nbf], Cout != C.
+ * expm by scaling and squaring with a degree-16 Taylor polynomial; the call
+ * reads one scalar (the 1-norm of Y) back to the host to choose the number
+ * of squarings, so it synchronises the stream once. */
+size_t gb_rotate_orbital_workspace_f64(int nbf);
+int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double* Cout, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
 /* ========================================================================
  * Split-product ("mixed") path on the tcgen05 tensor cores.
  *
@@ -179,8 +191,13 @@ int gb_energy_elec_f64(const double* elag, const double* C, const double* H, con
  * s + t <= nslices + 1 run as bf16 tcgen05 MMAs with FP32 accumulation in
  * TMEM, the leading product groups accumulated exactly.  nslices = 6 agrees
  * with FP64 to ~1e-12 normwise; nslices = 2 is the three-product bf16x3 split
- * (~1e-5).  Device status of these kernels: gb_device_status.
+ * (~1e-4).  nslices = GB_SPLIT_TF32X3 selects the three-product TF32 split
+ * instead (hi = tf32(x), lo = tf32(x - hi); hi hi + hi lo + lo hi as tf32
+ * tcgen05 MMAs, FP32 accumulation; ~1e-6).  Device status of these kernels:
+ * gb_device_status.
  * ====================================================================== */
+
+#define GB_SPLIT_TF32X3 32
 
 /* Status word of the tensor-core kernels on the current device: 0, or
  * GB_ERR_TIMEOUT when one of their bounded waits gave up.  Synchronises the

@@ -99,11 +99,12 @@ def integrals_mo_ri(C, H, b, P):
     N, _, Q = b.shape
     Hmat = C.T @ H @ C[:, :P]
     Cp = C[:, :P]
-    # T[q, m, l] = sum_n C[n, q] b[m, n, l] = sum_n C[n, q] b[n, m, l] (b symmetric
-    # is NOT assumed here: contract the second index explicitly)
-    T = np.einsum("nq,mnl->qml", Cp, b)
-    bmo = np.einsum("ma,qml->aql", C, T)
-    return Hmat, bmo
+    # T[q, m, l] = sum_n C[n, q] b[m, n, l] (b symmetric is NOT assumed here:
+    # contract the second index explicitly); both steps are batched BLAS GEMMs,
+    # as the reference's einsum(..., optimize=True) is
+    T = np.matmul(Cp.T[None, :, :], b).transpose(1, 0, 2)      # [m, q, l] -> [q, m, l]
+    bmo = np.matmul(C.T[None, :, :], T).transpose(1, 0, 2)      # [q, a, l] -> [a, q, l]
+    return Hmat, np.ascontiguousarray(bmo)
 
 
 def integrals_mo_full(C, H, I, P):
@@ -144,7 +145,7 @@ def lagrange2(n, cj12, ck12, C, H, I, b, p):
         w[na:P] += n[na:P, None] * bbk[na:P]
         w += cj12 @ bbk                                               # sum_q cj12[b,q] bMO[q,q,k]
         elag[:, :P] += n[None, :] * Hmat[:, :P]
-        elag[:, :P] += np.einsum("abk,bk->ab", bmo, w)
+        elag[:, :P] += np.matmul(bmo.transpose(1, 0, 2), w[:, :, None])[:, :, 0].T  # sum_k bMO[a,b,k] w[b,k]
         Y = ck12[:, :, None] * bmo[:P]                                # [b, q, k]
         elag[:, :P] -= bmo.reshape(N, -1) @ Y.reshape(P, -1).T
     else:

@@ -59,6 +59,8 @@ SIGNATURES = {
     "gb_lagrange_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_energy_elec_workspace_f64": (_Z, [_I, _I]),
     "gb_energy_elec_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_rotate_orbital_workspace_f64": (_Z, [_I]),
+    "gb_rotate_orbital_f64": (_I, [_P, _P, _I, _I, _P, _P, _Z, _P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
     "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
     "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),

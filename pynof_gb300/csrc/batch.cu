@@ -43,14 +43,6 @@ void mol_layout(Cv& c, int N, int P, int Q, int S, MolWs* w) {
   if (w) *w = MolWs{A, d, T, tf, dv};
 }
 
-struct SizeCarve2 {
-  size_t used = 0;
-  template <class T>
-  T* take(size_t n) {
-    used += align256(n * sizeof(T));
-    return nullptr;
-  }
-};
 
 // Prepared-b layout (must match gb_ri_prepare_mixed).
 void prepared_views(const void* prep, int N, int Q, int S, SlicedDesc* bT, SlicedDesc* bJ) {
@@ -65,7 +57,7 @@ int bn_of(int code) { return code == 1 ? 32 : code == 2 ? 64 : 128; }
 
 extern "C" size_t gb_jkj_batch_workspace_mixed(int nmol, const int* nbf, const int* nbf5, const int* naux,
                                                int nslices) {
-  SizeCarve2 c;
+  SizeCarve c;
   for (int i = 0; i < nmol; ++i) mol_layout(c, nbf[i], nbf5[i], naux[i], nslices, nullptr);
   c.used += 3 * ozaki_group_table_bytes(nmol);
   return c.used;
@@ -78,7 +70,8 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
   clear_error();
   GB_REQUIRE(nmol >= 1 && C && prep && nbf && nbf5 && naux && J && K && plan, GB_ERR_INVALID_ARG,
              "gb_jkj_batch_create_mixed: null argument");
-  GB_REQUIRE(nslices >= 1 && nslices <= 6, GB_ERR_INVALID_ARG, "gb_jkj_batch_create_mixed: nslices outside [1, 6]");
+  GB_REQUIRE(valid_split(nslices), GB_ERR_INVALID_ARG,
+             "gb_jkj_batch_create_mixed: nslices=%d is neither 1..6 nor GB_SPLIT_TF32X3", nslices);
   const int tcfg = tiles ? tiles[0] : 0, jcfg = tiles ? tiles[1] : 0;
   GB_REQUIRE(tcfg >= 0 && tcfg <= 3 && jcfg >= 0 && jcfg <= 3, GB_ERR_INVALID_ARG,
              "gb_jkj_batch_create_mixed: tile configuration outside [0, 3]");

@@ -39,6 +39,16 @@ struct Carve {
   }
 };
 
+// A Carve that only counts: run a layout function over it to size a workspace.
+struct SizeCarve {
+  size_t used = 0;
+  template <class T>
+  T* take(size_t count) {
+    used += align256(count * sizeof(T));
+    return nullptr;
+  }
+};
+
 // Size bookkeeping with the same rounding as Carve.
 struct Sizer {
   size_t used = 0;

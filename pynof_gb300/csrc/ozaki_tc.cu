@@ -40,16 +40,24 @@ constexpr int NUM_EPI_WARPS = 16, THREADS = 32 * (2 + NUM_EPI_WARPS);
 constexpr int MAX_REGS = 96;
 constexpr uint32_t TILE_BYTES = SL_TILE_BYTES;  // 4 KB per A slice tile (BM == SL_ROWS)
 
-template <int BN>
+// KIND 0: bf16 digit slices (kind::f16), four accumulators (three exact
+// groups and the FP32 group); KIND 1: TF32x3 (kind::tf32), two FP32
+// accumulators used alternately by consecutive chunks (one is drained while
+// the MMAs fill the other).
+template <int BN, int KIND>
 struct TileCfg {
   static_assert(BN == 32 || BN == 64 || BN == 128, "BN must be 32, 64 or 128");
-  static constexpr uint32_t B_TILE = BN * SL_K * 2;  // bytes of one B slice tile
-  static constexpr uint32_t TMEM_COLS = 4 * BN;      // power of two >= 32
-  static constexpr int CW = BN / 4;                  // columns per epilogue warp
-  // kind::f16 instruction descriptor: bf16 x bf16 -> f32, both K-major, M=128, N=BN
-  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+  static constexpr uint32_t B_TILE = BN * SL_K * 2;              // bytes of one B slice tile
+  static constexpr uint32_t TMEM_COLS = KIND ? 2 * BN : 4 * BN;  // power of two >= 32
+  static constexpr int CW = BN / 4;                              // columns per epilogue warp
+  static constexpr int KPER = KIND ? SL_K / 2 : SL_K;            // k per stage (one MMA)
+  static constexpr uint32_t FMT = KIND ? 2u : 1u;                // operand format: tf32 / bf16
+  // instruction descriptor: f32 accumulate, both operands K-major, M=128, N=BN
+  static constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) | ((uint32_t)(BN >> 3) << 17) |
                                     ((uint32_t)(BM >> 4) << 24);
 };
+// bytes of the per-tile assembly tables (see cta_tile)
+__host__ __device__ constexpr uint32_t epi_table_bytes(int BN) { return 20u * (uint32_t)(BM + BN); }
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
 constexpr float MAGIC = 12582912.0f;                          // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
@@ -142,6 +150,14 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
       : "memory");
 }
 
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                : "memory");
@@ -150,45 +166,68 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+// 8 consecutive TMEM columns of this warp's 32 lanes; complete after tmem_wait_ld().
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t (&v)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
                : "r"(taddr)
                : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld4_async(uint32_t taddr, uint32_t (&v)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+               : "r"(taddr)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Exact integer of an FP32 value x * 2^k with |x * 2^k| < 2^22 (rounded to
+// nearest even otherwise): adding 1.5 * 2^23 leaves the integer in the low
+// mantissa bits.  Pure FP32/ALU work, no float->int conversion unit.
+__device__ __forceinline__ int magic_int(float x, float scale) {
+  return __float_as_int(fmaf(x, scale, MAGIC)) - MAGIC_BITS;
 }
 
-// int64 fixed point z * 2^scale -> double, round to nearest even, integer ops only.
+// t * 2^frac rounded to nearest as a 64-bit integer, for |t| < 2^22 and
+// frac <= 16: rint(t) * 2^frac + rint((t - rint(t)) * 2^frac), both parts
+// through magic_int; (t - rint(t)) is exact.
+__device__ __forceinline__ long long split_round(float t, int frac, float two_frac) {
+  const float f1 = t + MAGIC;
+  const int ti = __float_as_int(f1) - MAGIC_BITS;
+  const int fi = magic_int(t - (f1 - MAGIC), two_frac);
+  return (long long)((unsigned long long)(long long)ti << frac) + fi;
+}
+
+// int64 fixed point z * 2^scale -> double, round to nearest even, integer ops
+// only (the FP64 pipe is narrow on this part).  The leading one is moved to
+// bit 63; the top 53 bits are the significand (implicit bit included, so adding
+// it to (exponent - 1) << 52 forms the exponent field and a rounding carry out
+// of the significand bumps the exponent), the low 11 bits decide the rounding.
 __device__ __forceinline__ double fixed_to_double(long long z, int scale, int negate) {
   if (z == 0) return 0.0;
-  unsigned long long sign = 0;
-  unsigned long long u = (unsigned long long)z;
-  if (z < 0) {
-    sign = 1ull << 63;
-    u = 0ull - u;
-  }
-  sign ^= (unsigned long long)(negate != 0) << 63;
-  int top = 63 - __clzll((long long)u);  // index of the leading one
-  unsigned long long mant;
-  if (top > 52) {
-    const int sh = top - 52;
-    mant = u >> sh;
-    const unsigned long long rem = u & ((1ull << sh) - 1);
-    const unsigned long long half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) {
-      ++mant;
-      if (mant == (1ull << 53)) {
-        mant >>= 1;
-        ++top;
-      }
-    }
-  } else {
-    mant = u << (52 - top);
-  }
-  const long long ef = (long long)top + scale + 1023;
-  if (ef <= 0) return __longlong_as_double((long long)sign);                           // underflow -> 0
-  if (ef >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));  // overflow -> inf
-  return __longlong_as_double((long long)(sign | ((unsigned long long)ef << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  const unsigned long long sign = (unsigned long long)((z < 0) != (negate != 0)) << 63;
+  const unsigned long long u = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
+  const int lz = __clzll((long long)u);
+  const unsigned long long m = u << lz;
+  const unsigned long long mant = m >> 11;
+  const uint32_t low = (uint32_t)m & 0x7FFu;
+  const unsigned long long up = (low > 0x400u || (low == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  const int ef = 63 - lz + scale + 1023;  // biased exponent of the leading one
+  if (ef <= 0) return __longlong_as_double((long long)sign);  // underflow -> signed zero
+  if (ef >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sign | ((((unsigned long long)(ef - 1)) << 52) + mant + up)));
+}
+
+// z * 2^scale as a double, negated when `negate`: the hardware int64 -> double
+// conversion (round to nearest even, as fixed_to_double) with the scale added
+// to the exponent field; results outside the normal range take the integer path.
+__device__ __forceinline__ double scaled_to_double(long long z, int scale, int negate) {
+  const long long b0 = __double_as_longlong(__ll2double_rn(z));
+  const int e0 = (int)((b0 >> 52) & 0x7FF) + scale;
+  if (z != 0 && e0 >= 1 && e0 <= 2046)
+    return __longlong_as_double((long long)(((unsigned long long)b0 + ((unsigned long long)(long long)scale << 52)) ^
+                                            ((unsigned long long)(negate != 0) << 63)));
+  return fixed_to_double(z, scale, negate);
 }
 
 struct KArgs {
@@ -201,22 +240,22 @@ struct KArgs {
 // tile s of A and t of B, whose descriptors differ from the stage's first tile
 // descriptors only in the start-address field.
 template <int S, int BN>
-__device__ __forceinline__ void issue_inexact(uint32_t tmem, uint64_t da, uint64_t db, bool& started) {
-  using T = TileCfg<BN>;
+__device__ __forceinline__ void issue_inexact(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool& started) {
+  using T = TileCfg<BN, 0>;
 #pragma unroll
   for (int s = 1; s <= S; ++s)
 #pragma unroll
     for (int t = 1; t <= S + 1 - s; ++t) {
       if (s + t <= 4) continue;
       mma_bf16(tmem + 3 * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)), db + (uint64_t)((t - 1) * (T::B_TILE >> 4)),
-               T::IDESC, started);
+               idesc, started);
       started = true;
     }
 }
 
 template <int S, int BN>
-__device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t db, bool first) {
-  using T = TileCfg<BN>;
+__device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool first) {
+  using T = TileCfg<BN, 0>;
   constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
 #pragma unroll
   for (int gg = 2; gg <= gE; ++gg) {
@@ -225,22 +264,39 @@ __device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t
       const int t = gg - s;
       if (s > S || t > S) continue;
       mma_bf16(tmem + (gg - 2) * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)),
-               db + (uint64_t)((t - 1) * (T::B_TILE >> 4)), T::IDESC, !(first && s == 1));
+               db + (uint64_t)((t - 1) * (T::B_TILE >> 4)), idesc, !(first && s == 1));
     }
   }
 }
 
-// Local tile index -> (batch, m0, n0), M tiles fastest so that the CTAs sharing
-// a B block run together (B read once from HBM, then from L2).  Returns false
+// TF32x3 products of one stage: hi hi + hi lo + lo hi into the one accumulator.
+template <int BN>
+__device__ __forceinline__ void issue_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool& started) {
+  using T = TileCfg<BN, 1>;
+  mma_tf32(tmem, da, db, idesc, started);
+  mma_tf32(tmem, da, db + (uint64_t)(T::B_TILE >> 4), idesc, true);
+  mma_tf32(tmem, da + (uint64_t)(TILE_BYTES >> 4), db, idesc, true);
+  started = true;
+}
+
+// Local tile index -> (batch, m0, n0).  The dimension with fewer tiles runs
+// fastest, so that the CTAs sharing a block of the large operand run together
+// (that block is read once from HBM, then from L2).  Returns false
 // for tiles a symmetric output does not need.
 template <int BN>
 __device__ __forceinline__ bool decode_tile(const OzGemm& g, long long t, int& bz, int& m0, int& n0) {
   const int mtiles = (g.M + BM - 1) / BM;
-  const long long per_batch = (long long)mtiles * ((g.N + BN - 1) / BN);
+  const int ntiles = (g.N + BN - 1) / BN;
+  const long long per_batch = (long long)mtiles * ntiles;
   bz = (int)(t / per_batch);
   const long long r = t % per_batch;
-  m0 = (int)(r % mtiles) * BM;
-  n0 = (int)(r / mtiles) * BN;
+  if (mtiles <= ntiles) {
+    m0 = (int)(r % mtiles) * BM;
+    n0 = (int)(r / mtiles) * BN;
+  } else {
+    n0 = (int)(r % ntiles) * BN;
+    m0 = (int)(r / ntiles) * BM;
+  }
   if (g.sym == SYM_ROWCOL && m0 > n0) return false;
   if (g.sym == SYM_PAIRCOL) {
     const int j1 = min(n0 + BN, g.N) - 1;
@@ -256,9 +312,9 @@ __device__ __forceinline__ bool decode_tile(const OzGemm& g, long long t, int& b
 }
 
 // One output tile, all roles.
-template <int S, int BN>
+template <int S, int BN, int KIND>
 __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0, unsigned char* smem_raw) {
-  using T = TileCfg<BN>;
+  using T = TileCfg<BN, KIND>;
   const OzGemm& g = a.g;
   constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
   constexpr bool has_inexact = (S + 1) > 4;
@@ -268,8 +324,15 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   // the assembly parks the tile's int64 results in the stage buffers
   constexpr uint32_t zs_bytes = BM * (BN + 1) * 8;
   constexpr uint32_t data_bytes = STAGES * stage_bytes > zs_bytes ? STAGES * stage_bytes : zs_bytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + data_bytes);
-  // bars: full[STAGES], empty[STAGES], accfull, accempty, done
+  // assembly tables: roff, mr [BM], coff, mc [BN] (int64), srow [BM], scol [BN] (int)
+  long long* e_roff = reinterpret_cast<long long*>(smem + data_bytes);
+  long long* e_mr = e_roff + BM;
+  long long* e_coff = e_mr + BM;
+  long long* e_mc = e_coff + BN;
+  int* e_srow = reinterpret_cast<int*>(e_mc + BN);
+  int* e_scol = e_srow + BM;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + data_bytes + epi_table_bytes(BN));
+  // bars: full[STAGES], empty[STAGES], accfull, accempty, done, (slot, flag), accfull1, accempty1
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
   const uint32_t sbase = smem_u32(smem);
@@ -278,6 +341,8 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   auto empty_bar = [&](int st) { return bar0 + 8u * (STAGES + st); };
   const uint32_t accfull_bar = bar0 + 8u * (2 * STAGES), accempty_bar = bar0 + 8u * (2 * STAGES + 1),
                  done_bar = bar0 + 8u * (2 * STAGES + 2);
+  // TF32x3: the second accumulator's pair (chunk c uses accumulator c & 1)
+  const uint32_t accfull1_bar = bar0 + 8u * (2 * STAGES + 6), accempty1_bar = bar0 + 8u * (2 * STAGES + 7);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -290,6 +355,8 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
     mbar_init(accfull_bar, 1);
     mbar_init(accempty_bar, NUM_EPI_WARPS);
     mbar_init(done_bar, 1);
+    mbar_init(accfull1_bar, 1);
+    mbar_init(accempty1_bar, NUM_EPI_WARPS);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -306,8 +373,13 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const int nkb = (g.K + BK - 1) / BK;
+  const int nkb = (g.K + T::KPER - 1) / T::KPER;
   const int nchunks = (nkb + CH - 1) / CH;
+  // A ragged last column tile runs its MMAs only as wide as it needs (N a
+  // multiple of 16 for M = 128); the idle epilogue warps skip their columns.
+  const int n_valid = min(BN, g.N - n0);
+  const int n_mma = (n_valid + 15) & ~15;
+  const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
 
   if (warp == 0) {
     // ---------------- producer ----------------
@@ -363,6 +435,25 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         tc_fence_after();
         const uint32_t sa = sbase + st * stage_bytes;
         const uint64_t da = desc_tile(sa, BM), db = desc_tile(sa + a_bytes, BN);
+        if constexpr (KIND == 1) {
+          // chunk c accumulates in buffer c & 1, drained by the epilogue while
+          // chunk c + 1 runs; before reusing a buffer wait for its last drain
+          const int c = kb / CH, bsel = c & 1;
+          if ((kb % CH) == 0) {
+            if (c >= 2) {
+              if (!mbar_wait(bsel ? accempty1_bar : accempty_bar, ((c >> 1) - 1) & 1, abort_flag)) {
+                signal_abort(abort_flag);
+                break;
+              }
+              tc_fence_after();
+            }
+            f_started = false;
+          }
+          issue_tf32<BN>(tmem + (uint32_t)(bsel * BN), da, db, idesc, f_started);
+          if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(bsel ? accfull1_bar : accfull_bar);
+          mma_commit(empty_bar(st));
+          continue;
+        }
         const int c = kb / CH;
         const bool first = (kb % CH) == 0;
         if (g.fdrain) {
@@ -375,9 +466,9 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
             tc_fence_after();
           }
           if (first) f_started = false;
-          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, f_started);
+          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
         } else {
-          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, f_started);
+          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
           if (first && c > 0) {
             if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
               signal_abort(abort_flag);
@@ -386,7 +477,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
             tc_fence_after();
           }
         }
-        issue_exact<S, BN>(tmem, da, db, first);
+        issue_exact<S, BN>(tmem, da, db, idesc, first);
         if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(accfull_bar);
         mma_commit(empty_bar(st));
       }
@@ -397,12 +488,72 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
     constexpr int CW = T::CW;
     const int q = warp & 3;
     const int cg = (warp - 2) >> 2;
+    const int et = threadIdx.x - 64;  // 0 .. 511
     const uint32_t lbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * CW);
+    const bool cols_live = cg * CW < n_valid;  // warp-uniform
+    // Row / column tables of the tile for the assembly, filled while the MMAs
+    // run: output offsets, mirror offsets (-1: none) and exponent scales.
+    {
+      const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
+      if (et < BM) {
+        const int i = m0 + et;
+        const bool in = i < g.M;
+        long long mr = -1;
+        if (in && g.sym == SYM_ROWCOL) mr = g.c_c.at(i);
+        if (in && g.sym == SYM_PAIRROW) {
+          const int mm = i / g.pair_n, nn = i % g.pair_n;  // the mirrored row of a pair-symmetric row
+          if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
+        }
+        e_roff[et] = in ? g.c_r.at(i) : 0;
+        e_mr[et] = mr;
+        e_srow[et] = in ? a.A.exps[abz * g.M + i] : 0;
+      } else if (et < BM + BN) {
+        const int c = et - BM, jj = n0 + c;
+        const bool in = jj < g.N;
+        long long mc = -1;
+        if (in && g.sym == SYM_ROWCOL) mc = g.c_r.at(jj);
+        if (in && g.sym == SYM_PAIRCOL) {
+          const int mm = jj / g.pair_n, nn = jj % g.pair_n;
+          if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
+        }
+        e_coff[c] = in ? g.c_c.at(jj) : 0;
+        e_mc[c] = mc;
+        e_scol[c] = in ? a.B.exps[bbz * g.N + jj] - (KIND ? 31 : 7 * gE + a.frac) : 0;
+      }
+    }
     long long R[CW];
 #pragma unroll
     for (int j = 0; j < CW; ++j) R[j] = 0;
+    const float two_frac = __int_as_float((127 + a.frac) << 23);  // 2^frac
+    const float upE = __int_as_float((127 + 7 * gE) << 23);       // 2^(7 gE)
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
+      if constexpr (KIND == 1) {
+        // R (units of 2^-31) += rint(F 2^31): |F| < 2^7 per chunk of 96 k
+        // (every |tf32 operand| < 1), so F 2^15 < 2^22 suits split_round
+        const int bsel = c & 1;
+        const bool got = mbar_wait(bsel ? accfull1_bar : accfull_bar, (c >> 1) & 1, abort_flag);
+        if (!__all_sync(0xffffffffu, got)) {
+          signal_abort(abort_flag);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        if (cols_live) {
+#pragma unroll
+          for (int h = 0; h < CW / 8; ++h) {
+            uint32_t v[8];
+            tmem_ld8_async(lbase + (uint32_t)(bsel * BN + h * 8), v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) R[h * 8 + j] += split_round(__uint_as_float(v[j]) * 32768.0f, 16, 65536.0f);
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bsel ? accempty1_bar : accempty_bar);
+        continue;
+      }
       const bool got = mbar_wait(accfull_bar, c & 1, abort_flag);
       if (!__all_sync(0xffffffffu, got)) {
         signal_abort(abort_flag);
@@ -411,29 +562,39 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       }
       tc_fence_after();
       const int fr = g.fdrain ? a.frac : 0;  // fraction bits carried by R from the start
-      for (int gg = 2; gg <= gE; ++gg) {
-        const float up = __int_as_float((127 + 7 * gg) << 23);  // 2^(7 g)
-        const int sh = 7 * (gE - gg) + fr;
 #pragma unroll
-        for (int h = 0; h < CW / 8; ++h) {
-          uint32_t v[8];
-          tmem_ld8(lbase + (uint32_t)((gg - 2) * BN + h * 8), v);
+      for (int h = 0; h < (cols_live ? CW / 4 : 0); ++h) {
+        // the exact groups' integers (|.| < 2^22 each), combined as
+        // sum_g i_g 2^(7 (gE - g)): groups 3 and 4 fit one int32 (< 2^30)
+        uint32_t v2[4], v3[4], v4[4];
+        tmem_ld4_async(lbase + (uint32_t)(h * 4), v2);
+        if (gE >= 3) tmem_ld4_async(lbase + (uint32_t)(BN + h * 4), v3);
+        if (gE >= 4) tmem_ld4_async(lbase + (uint32_t)(2 * BN + h * 4), v4);
+        tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const float f = fmaf(__uint_as_float(v[j]), up, MAGIC);
-            const long long iv = (long long)(__float_as_int(f) - MAGIC_BITS);
-            R[h * 8 + j] += (long long)((unsigned long long)iv << sh);
+        for (int j = 0; j < 4; ++j) {
+          const int i2 = magic_int(__uint_as_float(v2[j]), 16384.0f);  // 2^14
+          long long acc;
+          if (gE == 2) {
+            acc = i2;
+          } else if (gE == 3) {
+            acc = (long long)i2 * 128 + magic_int(__uint_as_float(v3[j]), 2097152.0f);  // 2^21
+          } else {
+            const int i34 = magic_int(__uint_as_float(v3[j]), 2097152.0f) * 128 +
+                            magic_int(__uint_as_float(v4[j]), 268435456.0f);  // 2^28
+            acc = (long long)i2 * 16384 + i34;
           }
+          R[h * 4 + j] += (long long)((unsigned long long)acc << fr);
         }
       }
-      if (has_inexact && g.fdrain) {
-        const float upEF = __int_as_float((127 + 7 * gE + a.frac) << 23);  // 2^(7 gE + frac)
+      if (has_inexact && g.fdrain && cols_live) {
 #pragma unroll
         for (int h = 0; h < CW / 8; ++h) {
           uint32_t v[8];
-          tmem_ld8(lbase + (uint32_t)(3 * BN + h * 8), v);
+          tmem_ld8_async(lbase + (uint32_t)(3 * BN + h * 8), v);
+          tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 8; ++j) R[h * 8 + j] += __float2ll_rn(__uint_as_float(v[j]) * upEF);
+          for (int j = 0; j < 8; ++j) R[h * 8 + j] += split_round(__uint_as_float(v[j]) * upE, a.frac, two_frac);
         }
       }
       tc_fence_before();
@@ -451,14 +612,19 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       // 1) fold the FP32 accumulator into the fixed point and park z in shared
       //    memory (the stage buffers are idle once every MMA has completed)
       const int row = q * 32 + lane;
-      const float upE = __int_as_float((127 + 7 * gE) << 23);
-      const float upF = __int_as_float((127 + a.frac) << 23);
       long long* Zs = reinterpret_cast<long long*>(smem);
 #pragma unroll
       for (int h = 0; h < CW / 8; ++h) {
         uint32_t v[8];
-        if (has_inexact && !g.fdrain) {
-          tmem_ld8(lbase + (uint32_t)(3 * BN + h * 8), v);
+        if constexpr (KIND == 1) {
+          // every chunk is already in R (fixed point, 31 fraction bits)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) Zs[row * (BN + 1) + cg * CW + h * 8 + j] = R[h * 8 + j];
+          continue;
+        }
+        if (has_inexact && !g.fdrain && cols_live) {
+          tmem_ld8_async(lbase + (uint32_t)(3 * BN + h * 8), v);
+          tmem_wait_ld();
         } else {
 #pragma unroll
           for (int j = 0; j < 8; ++j) v[j] = 0u;
@@ -466,39 +632,86 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           long long z = R[h * 8 + j];
-          if (!g.fdrain) {
-            const float t = __uint_as_float(v[j]) * upE;
-            const float th = rintf(t);
-            z = (long long)((unsigned long long)(z + __float2ll_rn(th)) << a.frac) + __float2ll_rn((t - th) * upF);
-          }
+          if (!g.fdrain) z = (long long)((unsigned long long)z << a.frac) + split_round(__uint_as_float(v[j]) * upE,
+                                                                                        a.frac, two_frac);
           Zs[row * (BN + 1) + cg * CW + h * 8 + j] = z;
         }
       }
       epi_barrier_any(false);
-      // 2) assemble FP64 and store, consecutive lanes on the unit-stride index
-      const int ew = warp - 2;  // 0..15
+      // 2) assemble FP64 and store; each thread keeps one column (lanes along
+      //    the columns) or one row (lanes along the rows), whichever index is
+      //    unit-stride in the output
       double* Cb = g.C + (long long)bz * g.c_sb;
-      const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
-      const int* ea_p = a.A.exps + abz * g.M;
-      const int* eb_p = a.B.exps + bbz * g.N;
       const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
       const bool rows_fast = g.c_c.div == 0 && g.c_c.s0 == 1 ? false : (g.c_r.div == 0 && g.c_r.s0 == 1);
-      for (int e = ew * 32 + lane; e < BM * BN; e += NUM_EPI_WARPS * 32) {
-        // element e -> (r, c): lanes along c (row-major outputs) or along r
-        const int r = rows_fast ? (e % BM) : (e / BN);
-        const int c = rows_fast ? (e / BM) : (e % BN);
-        const int i = m0 + r, jj = n0 + c;
-        if (i >= g.M || jj >= g.N) continue;
-        const double val = fixed_to_double(Zs[r * (BN + 1) + c], ea_p[i] + eb_p[jj] - 7 * gE - a.frac, g.negate);
-        Cb[g.c_r.at(i) + g.c_c.at(jj)] = val;
+      const int rlim = min(BM, g.M - m0), clim = min(BN, g.N - n0);
+      // one output element: convert and store (plus its mirror)
+      auto put = [&](long long z, int scale, long long ro, long long co, long long mr, long long mc) {
+        const double val = scaled_to_double(z, scale, g.negate);
+        Cb[ro + co] = val;
         if (mirror_rc) {
-          Cb[g.c_r.at(jj) + g.c_c.at(i)] = val;
+          Cb[mc + mr] = val;
         } else if (g.sym == SYM_PAIRCOL) {
-          const int mm = jj / g.pair_n, nn = jj % g.pair_n;
-          if (nn > mm) Cb[g.c_r.at(i) + g.c_c.at((long long)nn * g.pair_n + mm)] = val;
+          if (mc >= 0) Cb[ro + mc] = val;
         } else if (g.sym == SYM_PAIRROW) {
-          const int mm = i / g.pair_n, nn = i % g.pair_n;  // mirrored row of a pair-symmetric row
-          if (nn > mm) Cb[g.c_r.at((long long)nn * g.pair_n + mm) + g.c_c.at(jj)] = val;
+          if (mr >= 0) Cb[mr + co] = val;
+        }
+      };
+      constexpr int U = 4;  // elements in flight per thread
+      if (!rows_fast) {
+        constexpr int RSTEP = NUM_EPI_WARPS * 32 / BN;
+        constexpr int NIT = BM / RSTEP;
+        const int c = et % BN, r0 = et / BN;
+        if (c < clim) {
+          const int sc = e_scol[c];
+          const long long co = e_coff[c], mc = e_mc[c];
+          if (rlim == BM) {
+#pragma unroll 1
+            for (int it = 0; it < NIT; it += U) {
+              long long zv[U], ro[U], mr[U];
+              int sr[U];
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const int r = r0 + (it + u) * RSTEP;
+                zv[u] = Zs[r * (BN + 1) + c];
+                sr[u] = e_srow[r];
+                ro[u] = e_roff[r];
+                mr[u] = g.sym == SYM_NONE ? -1 : e_mr[r];
+              }
+#pragma unroll
+              for (int u = 0; u < U; ++u) put(zv[u], sr[u] + sc, ro[u], co, mr[u], mc);
+            }
+          } else {
+            for (int r = r0; r < rlim; r += RSTEP)
+              put(Zs[r * (BN + 1) + c], e_srow[r] + sc, e_roff[r], co, e_mr[r], mc);
+          }
+        }
+      } else {
+        constexpr int CSTEP = NUM_EPI_WARPS * 32 / BM;
+        constexpr int NIT = BN / CSTEP;
+        const int r = et % BM, c0 = et / BM;
+        if (r < rlim) {
+          const int sr = e_srow[r];
+          const long long ro = e_roff[r], mr = e_mr[r];
+          if (clim == BN && NIT % U == 0) {
+#pragma unroll 1
+            for (int it = 0; it < NIT; it += U) {
+              long long zv[U], co[U], mc[U];
+              int sc[U];
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const int c = c0 + (it + u) * CSTEP;
+                zv[u] = Zs[r * (BN + 1) + c];
+                sc[u] = e_scol[c];
+                co[u] = e_coff[c];
+                mc[u] = g.sym == SYM_NONE ? -1 : e_mc[c];
+              }
+#pragma unroll
+              for (int u = 0; u < U; ++u) put(zv[u], sr + sc[u], ro, co[u], mr, mc[u]);
+            }
+          } else {
+            for (int c = c0; c < clim; c += CSTEP) put(Zs[r * (BN + 1) + c], sr + e_scol[c], ro, e_coff[c], mr, e_mc[c]);
+          }
         }
       }
     }
@@ -515,18 +728,18 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   }
 }
 
-template <int S, int BN>
+template <int S, int BN, int KIND>
 __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs a) {
   extern __shared__ unsigned char smem_raw[];
   // a CTA of this or an earlier launch gave up: do not start (the host sees the status word)
   if (*(volatile int*)&g_tc_status != 0) return;
   int bz, m0, n0;
   if (!decode_tile<BN>(a.g, (long long)blockIdx.x + (long long)blockIdx.y * gridDim.x, bz, m0, n0)) return;
-  cta_tile<S, BN>(a, bz, m0, n0, smem_raw);
+  cta_tile<S, BN, KIND>(a, bz, m0, n0, smem_raw);
 }
 
 // Grouped launch: problem p owns the tiles [starts[p], starts[p + 1]).
-template <int S, int BN>
+template <int S, int BN, int KIND>
 __global__ void __maxnreg__(MAX_REGS)
     ozaki_grouped_kernel(const KArgs* __restrict__ probs, const long long* __restrict__ starts, int nprob) {
   extern __shared__ unsigned char smem_raw[];
@@ -541,16 +754,18 @@ __global__ void __maxnreg__(MAX_REGS)
   const KArgs& a = probs[lo];
   int bz, m0, n0;
   if (!decode_tile<BN>(a.g, t - starts[lo], bz, m0, n0)) return;
-  cta_tile<S, BN>(a, bz, m0, n0, smem_raw);
+  cta_tile<S, BN, KIND>(a, bz, m0, n0, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-size_t smem_bytes(int S, int BN) {
+// `code`: split code (1..6 digit slices or SPLIT_TF32X3)
+size_t smem_bytes(int code, int BN) {
+  const int S = form_of(code).S;
   const size_t stages = (size_t)STAGES * S * (TILE_BYTES + BN * SL_K * 2);
   const size_t zs = (size_t)BM * (BN + 1) * 8;
-  return (stages > zs ? stages : zs) + 256 + 1024;
+  return (stages > zs ? stages : zs) + epi_table_bytes(BN) + 256 + 1024;
 }
 
 using KernelFn = void (*)(KArgs);
@@ -559,24 +774,26 @@ using GroupedFn = void (*)(const KArgs*, const long long*, int);
 template <int BN>
 KernelFn single_for(int S) {
   switch (S) {
-    case 1: return ozaki_kernel<1, BN>;
-    case 2: return ozaki_kernel<2, BN>;
-    case 3: return ozaki_kernel<3, BN>;
-    case 4: return ozaki_kernel<4, BN>;
-    case 5: return ozaki_kernel<5, BN>;
-    default: return ozaki_kernel<6, BN>;
+    case 1: return ozaki_kernel<1, BN, 0>;
+    case 2: return ozaki_kernel<2, BN, 0>;
+    case 3: return ozaki_kernel<3, BN, 0>;
+    case 4: return ozaki_kernel<4, BN, 0>;
+    case 5: return ozaki_kernel<5, BN, 0>;
+    case SPLIT_TF32X3: return ozaki_kernel<2, BN, 1>;
+    default: return ozaki_kernel<6, BN, 0>;
   }
 }
 
 template <int BN>
 GroupedFn grouped_for(int S) {
   switch (S) {
-    case 1: return ozaki_grouped_kernel<1, BN>;
-    case 2: return ozaki_grouped_kernel<2, BN>;
-    case 3: return ozaki_grouped_kernel<3, BN>;
-    case 4: return ozaki_grouped_kernel<4, BN>;
-    case 5: return ozaki_grouped_kernel<5, BN>;
-    default: return ozaki_grouped_kernel<6, BN>;
+    case 1: return ozaki_grouped_kernel<1, BN, 0>;
+    case 2: return ozaki_grouped_kernel<2, BN, 0>;
+    case 3: return ozaki_grouped_kernel<3, BN, 0>;
+    case 4: return ozaki_grouped_kernel<4, BN, 0>;
+    case 5: return ozaki_grouped_kernel<5, BN, 0>;
+    case SPLIT_TF32X3: return ozaki_grouped_kernel<2, BN, 1>;
+    default: return ozaki_grouped_kernel<6, BN, 0>;
   }
 }
 
@@ -596,7 +813,7 @@ int configure_device() {
   std::lock_guard<std::mutex> lk(mu);
   if (dev < 0 || dev >= 64 || configured[dev]) return GB_OK;
   for (int bn : {32, 64, 128})
-    for (int sl = 1; sl <= 6; ++sl) {
+    for (int sl : {1, 2, 3, 4, 5, 6, SPLIT_TF32X3}) {
       const int sm = (int)smem_bytes(sl, bn);
       GB_TRY(cuda_status(cudaFuncSetAttribute(kernel_for(sl, bn), cudaFuncAttributeMaxDynamicSharedMemorySize, sm),
                          "cudaFuncSetAttribute"));
@@ -610,6 +827,7 @@ int configure_device() {
 
 // Fraction bits of the fixed-point assembly: keep |z| < 2^62.
 int frac_bits(int S, int K) {
+  if (S == SPLIT_TF32X3) return 0;
   const int nkb = (K + BK - 1) / BK;
   const int nchunks = (nkb + CH - 1) / CH;
   const int gE = S + 1 < 4 ? S + 1 : 4;
@@ -623,7 +841,9 @@ int frac_bits(int S, int K) {
 }
 
 int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
-  GB_REQUIRE(g.S >= 1 && g.S <= 6 && A.S == g.S && B.S == g.S, GB_ERR_INVALID_ARG, "ozaki_gemm: nslices mismatch");
+  const SliceForm f = form_of(g.S);
+  GB_REQUIRE(valid_split(g.S) && A.S == f.S && B.S == f.S && A.kind == f.kind && B.kind == f.kind,
+             GB_ERR_INVALID_ARG, "ozaki_gemm: split form mismatch (code %d)", g.S);
   GB_REQUIRE(g.bn == 32 || g.bn == 64 || g.bn == 128, GB_ERR_INVALID_ARG, "ozaki_gemm: N tile %d not in {32,64,128}",
              g.bn);
   GB_REQUIRE(A.rows == g.M && B.rows == g.N && A.K == g.K && B.K == g.K && (A.batch == g.batch || A.batch == 1) &&
@@ -643,7 +863,7 @@ int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
 
 KArgs make_args(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
   KArgs ka{g, A, B, frac_bits(g.S, g.K)};
-  if (g.K > 4096) ka.g.fdrain = 1;
+  if (g.K > 4096 && g.S != SPLIT_TF32X3) ka.g.fdrain = 1;
   return ka;
 }
 

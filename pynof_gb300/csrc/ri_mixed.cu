@@ -14,6 +14,28 @@ using namespace gb;
 
 namespace {
 
+// Orbitals on the N side of the tiles (the ragged last tile is only as wide as
+// it needs) when that pads less than 128-row tiles of orbitals: e.g. 300
+// orbitals take 304 columns instead of 384 rows.
+bool orbitals_on_n(long long P, long long rows) {
+  const long long rows128 = (rows + 127) / 128 * 128;
+  const long long normal = (P + 127) / 128 * 128 * rows128;
+  const long long swapped = rows128 * (P / 128 * 128 + ((P % 128) + 15) / 16 * 16);
+  return swapped < normal;
+}
+
+// T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)] from the sliced C^T (A, rows q) and b (bT)
+int half_transform_gemm(const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q, double* Tf, cudaStream_t s) {
+  OzGemm gt{};
+  gt.K = N; gt.batch = 1; gt.S = A.code(); gt.C = Tf; gt.c_sb = 0; gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
+  if (orbitals_on_n(P, (long long)N * Q)) {
+    gt.M = N * Q; gt.N = P; gt.c_r = lin(1); gt.c_c = lin((long long)N * Q);
+    return ozaki_gemm(bT, A, gt, s);
+  }
+  gt.M = P; gt.N = N * Q; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
+  return ozaki_gemm(A, bT, gt, s);
+}
+
 struct Prepared {
   SlicedDesc bT, bJ;
 };
@@ -28,19 +50,11 @@ void prepared_layout(C& c, int N, int Q, int S, Prepared* out) {
   }
 }
 
-struct SizeCarve {
-  size_t used = 0;
-  template <class T>
-  T* take(size_t n) {
-    used += align256(n * sizeof(T));
-    return nullptr;
-  }
-};
 
 int check_mixed(int N, int P, int Q, int S) {
   GB_REQUIRE(N > 0 && P > 0 && Q > 0 && P <= N, GB_ERR_BAD_SHAPE,
              "invalid sizes nbf=%d nbf5=%d naux=%d (need 0 < nbf5 <= nbf, naux > 0)", N, P, Q);
-  GB_REQUIRE(S >= 1 && S <= 6, GB_ERR_INVALID_ARG, "nslices=%d outside [1, 6]", S);
+  GB_REQUIRE(valid_split(S), GB_ERR_INVALID_ARG, "nslices=%d is neither 1..6 nor GB_SPLIT_TF32X3", S);
   GB_REQUIRE((long long)N * Q < 2147483647LL && (long long)N * N < 2147483647LL, GB_ERR_BAD_SHAPE,
              "sizes too large");
   return GB_OK;
@@ -67,6 +81,7 @@ void jkj_mixed_layout(C& c, int N, int P, int Q, int S, JkjMixedWs* w) {
     w->T = T;
   }
 }
+
 
 }  // namespace
 
@@ -121,19 +136,19 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   // A rows q over K = m: element C[m][q]
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
   // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
-  OzGemm gt{};
-  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = S;
-  gt.C = w.Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
-  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
-  GB_TRY(ozaki_gemm(w.A, pr.bT, gt, s));
+  GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, s));
   GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s));
   // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
   GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
   OzGemm gj{};
-  gj.M = P; gj.N = N * N; gj.K = Q; gj.batch = 1; gj.S = S;
-  gj.C = J; gj.c_sb = 0; gj.c_r = lin((long long)N * N); gj.c_c = lin(1);
-  gj.sym = SYM_PAIRCOL; gj.pair_n = N; gj.tag = "ozaki_tc:J";
-  GB_TRY(ozaki_gemm(w.d, pr.bJ, gj, s));
+  gj.K = Q; gj.batch = 1; gj.S = S; gj.C = J; gj.c_sb = 0; gj.pair_n = N; gj.tag = "ozaki_tc:J";
+  if (orbitals_on_n(P, (long long)N * N)) {
+    gj.M = N * N; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_PAIRROW;
+    GB_TRY(ozaki_gemm(pr.bJ, w.d, gj, s));
+  } else {
+    gj.M = P; gj.N = N * N; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_PAIRCOL;
+    GB_TRY(ozaki_gemm(w.d, pr.bJ, gj, s));
+  }
   // K[q] = T_q T_q^T
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s));
   OzGemm gk{};
@@ -174,7 +189,8 @@ extern "C" int gb_dgemm_mixed(const double* A, const double* B, int M, int N, in
                               void* workspace, size_t workspace_bytes, void* stream) {
   clear_error();
   GB_REQUIRE(M > 0 && N > 0 && K > 0, GB_ERR_BAD_SHAPE, "gb_dgemm_mixed: bad sizes M=%d N=%d K=%d", M, N, K);
-  GB_REQUIRE(nslices >= 1 && nslices <= 6, GB_ERR_INVALID_ARG, "gb_dgemm_mixed: nslices=%d outside [1, 6]", nslices);
+  GB_REQUIRE(valid_split(nslices), GB_ERR_INVALID_ARG, "gb_dgemm_mixed: nslices=%d is neither 1..6 nor GB_SPLIT_TF32X3",
+             nslices);
   GB_REQUIRE(A && B && C, GB_ERR_INVALID_ARG, "gb_dgemm_mixed: null pointer");
   GB_REQUIRE(workspace_bytes >= gb_dgemm_mixed_workspace(M, N, K, nslices), GB_ERR_WORKSPACE,
              "gb_dgemm_mixed: workspace too small");
@@ -240,11 +256,7 @@ int hcore_f64(const double* C, const double* H, int N, int P, double* X, double*
 int half_transform_mixed(const double* C, const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q,
                          double* Tf, cudaStream_t s) {
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, A, s));
-  OzGemm gt{};
-  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = A.S;
-  gt.C = Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
-  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
-  return ozaki_gemm(A, bT, gt, s);
+  return half_transform_gemm(A, bT, N, P, Q, Tf, s);
 }
 }  // namespace
 
@@ -274,10 +286,14 @@ extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* 
   // T read with rows l and K = n: element T[p][n][l]
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
   OzGemm gq{};
-  gq.M = P; gq.N = Q; gq.K = N; gq.batch = P; gq.S = S;
-  gq.C = w.bpq; gq.c_sb = (long long)P * Q; gq.c_r = lin(Q); gq.c_c = lin(1);
-  gq.sym = SYM_NONE; gq.tag = "ozaki_tc:bpq";
-  GB_TRY(ozaki_gemm(w.A, w.Tt, gq, s));
+  gq.K = N; gq.batch = P; gq.S = S; gq.C = w.bpq; gq.c_sb = (long long)P * Q; gq.sym = SYM_NONE; gq.tag = "ozaki_tc:bpq";
+  if (orbitals_on_n(P, Q)) {
+    gq.M = Q; gq.N = P; gq.c_r = lin(1); gq.c_c = lin(Q);
+    GB_TRY(ozaki_gemm(w.Tt, w.A, gq, s));
+  } else {
+    gq.M = P; gq.N = Q; gq.c_r = lin(Q); gq.c_c = lin(1);
+    GB_TRY(ozaki_gemm(w.A, w.Tt, gq, s));
+  }
   GB_TRY(launch_gather_diag(w.bpq, w.d, P, Q, (long long)P * Q + Q, s));
   GemmF64 gj{};
   gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1;
@@ -353,11 +369,7 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Aall, s));
   SlicedDesc Ap = w.Aall;
   Ap.rows = P;
-  OzGemm gt{};
-  gt.M = P; gt.N = N * Q; gt.K = N; gt.batch = 1; gt.S = S;
-  gt.C = w.Tf; gt.c_sb = 0; gt.c_r = lin((long long)N * Q); gt.c_c = lin(1);
-  gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
-  GB_TRY(ozaki_gemm(Ap, pr.bT, gt, s));
+  GB_TRY(half_transform_gemm(Ap, pr.bT, N, P, Q, w.Tf, s));
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
   // bMO[a][q][l] (batch q)
   OzGemm gm{};

@@ -115,12 +115,82 @@ __global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, Slice
   }
 }
 
+// TF32 hi / lo of y = x 2^-E (|x| < 2^E), as FP32 bit patterns: hi = tf32(y),
+// lo = tf32(y - hi), each rounded to nearest even to 11 significant bits from
+// the FP64 bits with integer arithmetic (y - hi is exact); values below the
+// FP32 normal range are flushed to zero.
+__device__ __forceinline__ void tf32_split(double x, int E, uint32_t& hi, uint32_t& lo) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(bits >> 63);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  hi = 0u;
+  lo = 0u;
+  if (ex == 0) return;  // zero (FP64 subnormals are far below the FP32 range after scaling)
+  const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);  // y = m 2^(ex - 1075 - E)
+  int fe = ex - E - 1023 + 127;
+  unsigned long long q = m >> 42;
+  const unsigned long long rem = m & ((1ull << 42) - 1), half = 1ull << 41;
+  if (rem > half || (rem == half && (q & 1ull))) ++q;
+  const long long r = (long long)m - (long long)(q << 42);  // |r| <= 2^41
+  if (q == (1ull << 11)) {
+    q >>= 1;
+    ++fe;
+  }
+  if (fe > 0) hi = (sign << 31) | ((uint32_t)fe << 23) | (((uint32_t)q & 0x3FFu) << 13);
+  if (r == 0 || fe <= 0) return;
+  const uint32_t rs = sign ^ (r < 0 ? 1u : 0u);
+  const unsigned long long ra = (unsigned long long)(r < 0 ? -r : r);
+  int top = 63 - __clzll((long long)ra);  // leading one of |r|
+  unsigned long long q2;
+  if (top > 10) {
+    const int sh = top - 10;
+    q2 = ra >> sh;
+    const unsigned long long rem2 = ra & ((1ull << sh) - 1), h2 = 1ull << (sh - 1);
+    if (rem2 > h2 || (rem2 == h2 && (q2 & 1ull))) ++q2;
+    if (q2 == (1ull << 11)) {
+      q2 >>= 1;
+      ++top;
+    }
+  } else {
+    q2 = ra << (10 - top);
+  }
+  const int fe2 = ex - 1075 - E + top + 127;
+  if (fe2 > 0) lo = (rs << 31) | ((uint32_t)fe2 << 23) | (((uint32_t)q2 & 0x3FFu) << 13);
+}
+
+// TF32x3 planes, one CTA of 256 threads per (row block, k block of 8): thread
+// -> (row r, k group of 4), 16-byte stores per plane (same thread map as the
+// bf16 digits).
+__global__ void __launch_bounds__(256) tf32_blocked_kernel(SliceSrc src, SlicedDesc dst) {
+  const long long b = blockIdx.y;
+  const int kbn = dst.kblocks();
+  const int rb = blockIdx.x / kbn, kb = blockIdx.x % kbn;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ri = lane & 7, kg = warp >> 2, rg = (warp & 3) * 4 + (lane >> 3);
+  const int r = rb * SL_ROWS + rg * 8 + ri;
+  const int k0 = kb * (SL_K / 2) + kg * 4;
+  const bool rok = r < dst.rows;
+  const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
+  const int e = rok ? dst.exps[b * dst.rows + r] : 0;
+  uint32_t hi[4], lo[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int k = k0 + u;
+    tf32_split((rok && k < dst.K) ? base[src.k.at(k)] : 0.0, e, hi[u], lo[u]);
+  }
+  unsigned char* out = reinterpret_cast<unsigned char*>(dst.planes) + b * dst.batch_bytes() +
+                       ((long long)blockIdx.x * 2) * SL_TILE_BYTES + (kg * 16 + rg) * 128 + ri * 16;
+  *reinterpret_cast<uint4*>(out) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+  *reinterpret_cast<uint4*>(out + SL_TILE_BYTES) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+}
+
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace
 
 int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
-  GB_REQUIRE(dst.S >= 1 && dst.S <= 6, GB_ERR_INVALID_ARG, "slice_operand: nslices=%d outside [1, 6]", dst.S);
+  GB_REQUIRE((dst.kind == 0 && dst.S >= 1 && dst.S <= 6) || (dst.kind == 1 && dst.S == 2), GB_ERR_INVALID_ARG,
+             "slice_operand: bad split form (planes %d, kind %d)", dst.S, dst.kind);
   GB_REQUIRE(dst.batch >= 1 && dst.batch <= 65535 && dst.rows >= 0, GB_ERR_BAD_SHAPE, "slice_operand: bad batch");
   GB_REQUIRE((reinterpret_cast<uintptr_t>(dst.planes) & 15) == 0, GB_ERR_INVALID_ARG,
              "slice_operand: planes not 16-byte aligned");
@@ -135,6 +205,10 @@ int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
   const long long blocks = (long long)dst.rblocks() * dst.kblocks();
   GB_REQUIRE(blocks <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many blocks");
   const dim3 grid((unsigned)blocks, dst.batch);
+  if (dst.kind == 1) {
+    GB_LAUNCH("slice_tf32", s, tf32_blocked_kernel<<<grid, 256, 0, s>>>(src, dst));
+    return GB_OK;
+  }
   switch (dst.S) {
     case 1: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<1><<<grid, 256, 0, s>>>(src, dst)); break;
     case 2: GB_LAUNCH("slice_digits", s, digits_blocked_kernel<2><<<grid, 256, 0, s>>>(src, dst)); break;

@@ -23,6 +23,14 @@
 //   byte(r, k) = ((k / 8) * 16 + r / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
 // Blocks are ordered [batch][rb][kb].  Rows and K are zero-padded to whole
 // blocks.  Exponents: exps[b][r] (int32).
+//
+// TF32x3 form (split code SPLIT_TF32X3): two planes, hi = tf32(x 2^-E) and
+// lo = tf32(x 2^-E - hi) (each rounded to nearest even, 11 significant bits,
+// FP32 exponent), for the classic three-product TF32 split (hi hi + hi lo +
+// lo hi with FP32 accumulation).  A block is then 128 rows x 8 k of 32-bit
+// elements, the same 4 KB tiles and core-matrix order with 4 elements per
+// 16-byte core-matrix row:
+//   byte(r, k) = ((k / 4) * 16 + r / 8) * 128 + (r % 8) * 16 + (k % 4) * 4.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -35,6 +43,16 @@ constexpr int SL_ROWS = 128;               // rows per block
 constexpr int SL_K = 16;                   // K per block
 constexpr int SL_TILE_BYTES = SL_ROWS * SL_K * 2;  // one slice of one block: 4 KB
 
+// Split codes ("nslices" in the C ABI): 1..6 bf16 digit slices, or the TF32x3 split.
+constexpr int SPLIT_TF32X3 = 32;
+struct SliceForm {
+  int S, kind;  // planes; 0 = bf16 digits, 1 = tf32 hi/lo
+};
+__host__ __device__ inline bool valid_split(int code) { return (code >= 1 && code <= 6) || code == SPLIT_TF32X3; }
+__host__ __device__ inline SliceForm form_of(int code) {
+  return code == SPLIT_TF32X3 ? SliceForm{2, 1} : SliceForm{code, 0};
+}
+
 struct SliceSrc {
   const double* p;
   long long sb;  // batch stride
@@ -43,27 +61,33 @@ struct SliceSrc {
 };
 
 struct SlicedDesc {
-  __nv_bfloat16* planes;  // blocked digit tiles
+  __nv_bfloat16* planes;  // blocked digit tiles (32-bit elements when kind == 1)
   int* exps;              // [batch][rows]
   int batch, rows, K, S;
+  int kind = 0;  // 0: bf16 digits, 16 k per block; 1: tf32 hi/lo, 8 k per block
+  __host__ __device__ int kper() const { return kind ? SL_K / 2 : SL_K; }
+  __host__ __device__ int code() const { return kind ? SPLIT_TF32X3 : S; }  // the split code it was cut with
   __host__ __device__ int rblocks() const { return (rows + SL_ROWS - 1) / SL_ROWS; }
-  __host__ __device__ int kblocks() const { return (K + SL_K - 1) / SL_K; }
+  __host__ __device__ int kblocks() const { return (K + kper() - 1) / kper(); }
   __host__ __device__ long long block_bytes() const { return (long long)S * SL_TILE_BYTES; }
   __host__ __device__ long long batch_bytes() const { return (long long)rblocks() * kblocks() * block_bytes(); }
 };
 
-inline size_t sliced_plane_bytes(int batch, int rows, int K, int S) {
-  SlicedDesc d{nullptr, nullptr, batch, rows, K, S};
+// `code` is a split code (1..6 or SPLIT_TF32X3).
+inline size_t sliced_plane_bytes(int batch, int rows, int K, int code) {
+  const SliceForm f = form_of(code);
+  SlicedDesc d{nullptr, nullptr, batch, rows, K, f.S, f.kind};
   return (size_t)batch * d.batch_bytes();
 }
 inline size_t sliced_exp_bytes(int batch, int rows) { return (size_t)batch * rows * sizeof(int); }
 
 // Carve a sliced operand (planes + exponents) out of a workspace or buffer.
 template <class Cv>
-SlicedDesc take_sliced(Cv& c, int batch, int rows, int K, int S) {
-  auto* p = c.template take<unsigned char>(sliced_plane_bytes(batch, rows, K, S));
+SlicedDesc take_sliced(Cv& c, int batch, int rows, int K, int code) {
+  auto* p = c.template take<unsigned char>(sliced_plane_bytes(batch, rows, K, code));
   auto* e = c.template take<int>((size_t)batch * rows);
-  return SlicedDesc{reinterpret_cast<__nv_bfloat16*>(p), e, batch, rows, K, S};
+  const SliceForm f = form_of(code);
+  return SlicedDesc{reinterpret_cast<__nv_bfloat16*>(p), e, batch, rows, K, f.S, f.kind};
 }
 
 // Exponents then digits; both kernels read the source once.

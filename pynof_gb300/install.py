@@ -70,7 +70,10 @@ def install(pynof) -> dict:
     pynof.compute_integrals = compute_integrals
     # computeLagrange2 and ENERGY1r hold cupy code inline (utils.py:272-327),
     # so they are replaced whole; the reference CPU branch stays behind p.gpu=False
-    for name, gpu_fn in (("computeLagrange2", utils.computeLagrange2), ("ENERGY1r", utils.ENERGY1r)):
+    # rotate_orbital (utils.py:550-565) runs scipy expm on the host: on the
+    # device path it becomes the FP64 device rotation
+    for name, gpu_fn in (("computeLagrange2", utils.computeLagrange2), ("ENERGY1r", utils.ENERGY1r),
+                         ("rotate_orbital", utils.rotate_orbital)):
         cpu_fn = getattr(pynof.utils, name)
         saved["utils." + name] = cpu_fn
         saved["pynof." + name] = getattr(pynof, name)

@@ -24,8 +24,9 @@ import torch
 
 from . import ops
 
-#: Arithmetic of the device path: "fp64" (DMMA) or "mixed" (tcgen05 digit
-#: slices; nslices=6 agrees with FP64 to ~1e-11, nslices=2 is bf16x3).
+#: Arithmetic of the device path: "fp64" (DMMA) or "mixed" (tcgen05 split
+#: products; nslices=6 bf16 digit slices agree with FP64 to ~1e-11, nslices=2
+#: is bf16x3, nslices=ops.SPLIT_TF32X3 is tf32x3).
 PRECISION = {"mode": "mixed", "nslices": 6}
 
 _prep_lock = threading.Lock()
@@ -36,8 +37,8 @@ _prepared: dict = {}
 def set_precision(mode: str, nslices: int = 6) -> None:
     if mode not in ("fp64", "mixed"):
         raise ValueError(f"unknown precision mode {mode!r}")
-    if not 1 <= nslices <= 6:
-        raise ValueError("nslices must be in [1, 6]")
+    if not (1 <= nslices <= 6 or nslices == ops.SPLIT_TF32X3):
+        raise ValueError(f"nslices must be in [1, 6] or ops.SPLIT_TF32X3 ({ops.SPLIT_TF32X3})")
     PRECISION["mode"] = mode
     PRECISION["nslices"] = nslices
 

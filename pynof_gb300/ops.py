@@ -265,6 +265,20 @@ def energy_elec(elag, C, H, n, nbeta: int, nalpha: int, high_spin: bool = False)
     return E
 
 
+def rotate_orbital(y: torch.Tensor, C: torch.Tensor, nbf5: int) -> torch.Tensor:
+    """C expm(Y) (rotate_orbital) with Y the antisymmetric matrix of the packed
+    step y (rows i < nbf5 of the strict upper triangle, row-major)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    nvar = N * (N - 1) // 2 - (N - nbf5) * (N - nbf5 - 1) // 2
+    _require(y, (nvar,), "y")
+    dev = C.device
+    out = torch.empty_like(C)
+    wp, wn = _ws("gb_rotate_orbital_workspace_f64", N, device=dev)
+    _lib.call("gb_rotate_orbital_f64", _ptr(y), _ptr(C), N, nbf5, _ptr(out), wp, wn, _stream(dev))
+    return out
+
+
 # ----------------------------------------------------------------------------
 # split-product tensor-core path
 # ----------------------------------------------------------------------------
@@ -273,6 +287,11 @@ def check_device_status() -> None:
     st = _lib.device_status(reset=True)
     if st != 0:
         raise _lib.GBError(st, "a tensor-core kernel gave up on a bounded wait")
+
+
+#: Split code of the three-product TF32 form (``GB_SPLIT_TF32X3``), accepted
+#: wherever ``nslices`` is (1..6 select bf16 digit slices).
+SPLIT_TF32X3 = 32
 
 
 def dgemm_mixed(A: torch.Tensor, B: torch.Tensor, nslices: int = 6) -> torch.Tensor:

@@ -5,9 +5,9 @@ Restates the orbital / occupation optimisation of ``pynof.compute_energy``
 over the softmax gammas), ``orbopt_adam`` (``minimization.py:200-253``,
 AMSgrad on orbital rotations), ``order_occupations_softmax``
 (``guess.py:77-106``) and the convergence test on the two gradient norms --
-with every four-index contraction (``computeJKH_MO``, ``computeLagrange2``) on
-the GPU and the occupation-space / rotation math in FP64 on the host
-(:mod:`pynof_gb300.nof`).
+with every four-index contraction (``computeJKH_MO``, ``computeLagrange2``)
+and the orbital rotation (``rotate_orbital``, FP64 expm) on the GPU and the
+occupation-space math in FP64 on the host (:mod:`pynof_gb300.nof`).
 
 A :class:`Backend` owns one molecule's resident device state (b, its sliced
 form for the tensor-core path, H) and a CUDA stream, so several solves can
@@ -75,6 +75,12 @@ class Backend:
                 res = ops.jkh_mo_ri(dC, self.H, self.b, P)
             return self._sync_host(*res)
 
+    def rotate(self, y, C):
+        """C expm(Y) on the device (FP64), host in / host out."""
+        with torch.cuda.stream(self.stream):
+            out = ops.rotate_orbital(ops.to_device(y, self.device), ops.to_device(C, self.device), self.st.nbf5)
+            return self._sync_host(out)[0]
+
     def lagrange2(self, C, n, cj12, ck12):
         self.calls["lagrange2"] += 1
         st = self.st
@@ -99,14 +105,14 @@ class SolveState:
 
 def calcorbe(y, n, cj12, ck12, C, be, p):
     """``pnof.py:1103-1111``."""
-    Cn = C if not np.any(y) else nof.rotate_orbital(y, C, p)
+    Cn = C if not np.any(y) else be.rotate(y, C)
     J_MO, K_MO, H_core = be.jkh_mo(Cn)
     return nof.calce(n, cj12, ck12, J_MO, K_MO, H_core, p)
 
 
 def calcorbg(y, n, cj12, ck12, C, be, p):
     """``pnof.py:1114-1131``."""
-    Cn = C if not np.any(y) else nof.rotate_orbital(y, C, p)
+    Cn = C if not np.any(y) else be.rotate(y, C)
     np.fill_diagonal(cj12, 0.0)
     np.fill_diagonal(ck12, 0.0)
     elag, _ = be.lagrange2(Cn, n, cj12, ck12)
@@ -151,7 +157,7 @@ def orbopt_adam(gamma, C, be, p, state: SolveState):
         vhat = v / (1.0 - beta2 ** (i + 1))
         vhat_max = np.maximum(vhat_max, vhat)
         y = -alpha * mhat / np.sqrt(vhat_max + 1e-8)
-        C = nof.rotate_orbital(y, C, p)
+        C = be.rotate(y, C)
         E = calcorbe(y0, n, cj12, ck12, C, be, p)
         if E < best_E:
             best_C, best_E = C, E

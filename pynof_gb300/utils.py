@@ -61,6 +61,15 @@ def computeF_RC_driver(J, K, n, H, cj12, ck12, p):
     return computeF_RC_GPU(J, K, n, H, cj12, ck12, p)
 
 
+def rotate_orbital(y, C, p):
+    """``pynof/utils.py:550-565``: C expm(Y) from the packed step y, on the
+    device in FP64 (the reference builds Y in a Python loop and calls
+    scipy.linalg.expm).  Host numpy in, host numpy out."""
+    Cd = as_device(C)
+    yd = as_device(np.asarray(y, dtype=np.float64).reshape(-1))
+    return to_host(ops.rotate_orbital(yd, Cd, p.nbf5))
+
+
 def computeLagrangeConvergency(elag):
     """sumdiff, maxdiff of |elag - elag^T| -- ``pynof/utils.py:405-411``."""
     d = np.abs(elag - elag.T)

@@ -51,6 +51,20 @@ def test_workspace_queries(lib):
     assert _lib.query("gb_lagrange2_ri_workspace_f64", N, P, Q) >= 2 * N * P * Q * 8
 
 
+def test_split_codes(lib):
+    """GB_SPLIT_TF32X3 in the header is ops.SPLIT_TF32X3, and its prepared
+    factor (two 32-bit planes) is smaller than six bf16 digit planes."""
+    from pynof_gb300 import _lib, ops
+
+    hdr = open(HEADER).read()
+    m = re.search(r"#define\s+GB_SPLIT_TF32X3\s+(\d+)", hdr)
+    assert m and int(m.group(1)) == ops.SPLIT_TF32X3
+    N, Q = 600, 2400
+    tf = _lib.query("gb_ri_prepare_bytes_mixed", N, Q, ops.SPLIT_TF32X3)
+    s6 = _lib.query("gb_ri_prepare_bytes_mixed", N, Q, 6)
+    assert 2 * N * N * Q * 8 <= tf < s6
+
+
 def test_version_and_error(lib):
     assert lib.gb_version() >= 100
     assert isinstance(lib.gb_last_error(), bytes)

@@ -21,8 +21,10 @@ def fake_pynof():
         setattr(pynof, attr, fn)
     pynof.utils.computeLagrange2 = lambda *a: ("reference-cpu", "computeLagrange2")
     pynof.utils.ENERGY1r = lambda *a: ("reference-cpu", "ENERGY1r")
+    pynof.utils.rotate_orbital = lambda *a: ("reference-cpu", "rotate_orbital")
     pynof.computeLagrange2 = pynof.utils.computeLagrange2
     pynof.ENERGY1r = pynof.utils.ENERGY1r
+    pynof.rotate_orbital = pynof.utils.rotate_orbital
     pynof.integrals.compute_integrals = lambda wfn, mol, p: (1, 2, 3, 4, [], [], 7)
     pynof.compute_integrals = pynof.integrals.compute_integrals
     return pynof
@@ -42,6 +44,8 @@ def test_install_rebinds_and_restores():
     p = types.SimpleNamespace(gpu=False)
     assert pynof.computeLagrange2(1, 2, 3, 4, 5, 6, 7, p) == ("reference-cpu", "computeLagrange2")
     assert pynof.utils.ENERGY1r(1, 2, 3, 4, 5, 6, 7, p) == ("reference-cpu", "ENERGY1r")
+    assert pynof.rotate_orbital(1, 2, p) == ("reference-cpu", "rotate_orbital")
+    assert "p.gpu" in (pynof.rotate_orbital.__doc__ or "")  # the installed dispatcher
     # compute_integrals with p.gpu=False is the reference's
     assert pynof.compute_integrals(None, None, p) == (1, 2, 3, 4, [], [], 7)
     inst.uninstall(pynof, saved)
@@ -49,6 +53,7 @@ def test_install_rebinds_and_restores():
         mod, attr = d.split(".")
         assert getattr(getattr(pynof, mod), attr) is fn
     assert pynof.computeLagrange2(1, 2, 3, 4, 5, 6, 7, p) == ("reference-cpu", "computeLagrange2")
+    assert pynof.rotate_orbital(1, 2, p) == ("reference-cpu", "rotate_orbital")
 
 
 def test_precision_switch():
