@@ -138,6 +138,27 @@ size_t gb_mo_full_workspace_f64(int nbf, int nbf5);
 int gb_mo_full_f64(const double* C, const double* H, const double* I, int nbf, int nbf5, double* Hmat,
                    double* I_MO, void* workspace, size_t workspace_bytes, void* stream);
 
+/* The RI factor from the three-centre integrals: b[m][n][l] = sum_k mnk[m][n][k]
+ * M[k][l] with M = metric^(-1/2) [naux][naux] (symmetric).  Replaces the
+ * einsum "mnk,kl->mnl" of compute_integrals (pynof/integrals.py:49); the
+ * metric power itself (psi4's Matrix::power(-0.5, 1e-14), :45) stays on the
+ * host in FP64.  The split-product form of the same contraction is
+ * gb_dgemm_mixed(mnk, M, nbf*nbf, naux, naux, ...) (M symmetric). */
+int gb_ri_factor_f64(const double* mnk, const double* M, int nbf, int naux, double* b, void* stream);
+
+/* HF-JK helpers (pynof/integrals.py:490-562).
+ * gb_density_hf_f64: D [nbf][nbf] = sum_{j0 <= j < j1} C[:, j] C[:, j]^T.
+ *   Replaces computeD_HF (j in [0, nbeta), integrals.py:493-500) and
+ *   computeDalpha_HF (j in [nbeta, nalpha), :503-510).
+ * gb_jk_hf_full_f64: J[m][n] = sum_sl D[l][s] I[m][n][s][l],
+ *   K[m][s] = sum_nl D[n][l] I[m][n][s][l], for a symmetric D (as the two
+ *   density functions build it).  Replaces JK_HF_Full_GPU (:537-543) and,
+ *   with the alpha density, JKalpha_HF_Full_GPU (:557-562). */
+int gb_density_hf_f64(const double* C, int nbf, int j0, int j1, double* D, void* stream);
+size_t gb_jk_hf_full_workspace_f64(int nbf);
+int gb_jk_hf_full_f64(const double* D, const double* I, int nbf, double* J, double* K, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
 /* A6  computeLagrange2, full ERI, closed shell (pynof/utils.py:302-326).  The
  *     diagonals of cj12 / ck12 are ignored. */
 size_t gb_lagrange2_full_workspace_f64(int nbf, int nbf5);
@@ -176,12 +197,28 @@ int gb_energy_elec_f64(const double* elag, const double* C, const double* H, con
  * scipy.linalg.expm.  y: the packed step, nvar = nbf (nbf - 1) / 2 -
  * (nbf - nbf5) (nbf - nbf5 - 1) / 2 values over (i < nbf5, j > i) in row-major
  * order (Y[i][j] = y, Y[j][i] = -y); C, Cout: [nbf][nbf], Cout != C.
- * expm by scaling and squaring with a degree-16 Taylor polynomial; the call
- * reads one scalar (the 1-norm of Y) back to the host to choose the number
- * of squarings, so it synchronises the stream once. */
+ * expm by scaling and squaring with a degree-16 Taylor polynomial; the number
+ * of squarings follows from norm1, an upper bound of ||Y||_1 (max column sum
+ * of |Y|) the caller knows from y.  norm1 < 0: the call measures ||Y||_1 on
+ * the device and reads it back, synchronising the stream once.  With
+ * norm1 >= 0 it launches only (it can be captured in a CUDA graph, which
+ * then holds for every y whose bound needs the same number of squarings). */
 size_t gb_rotate_orbital_workspace_f64(int nbf);
-int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double* Cout, void* workspace,
-                          size_t workspace_bytes, void* stream);
+int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double norm1, double* Cout,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* Capture of the calling thread's work on a (non-default) stream into a CUDA
+ * graph, thread-local capture mode: gb_graph_begin, then any of this
+ * library's calls that neither allocate nor synchronise (preallocated
+ * outputs and workspaces; gb_rotate_orbital_f64 with norm1 >= 0), then
+ * gb_graph_end; gb_graph_launch replays.  No counterpart in the reference
+ * (PyNOF issues every cupy call eagerly); used by the serving loop to make
+ * one orbital step one launch. */
+typedef struct gb_graph gb_graph;
+int gb_graph_begin(void* stream);
+int gb_graph_end(void* stream, gb_graph** graph);
+int gb_graph_launch(gb_graph* graph, void* stream);
+int gb_graph_destroy(gb_graph* graph);
 
 /* ========================================================================
  * Split-product ("mixed") path on the tcgen05 tensor cores.

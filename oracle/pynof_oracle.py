@@ -261,6 +261,42 @@ def rotate_orbital(y, C, p):
     return C @ scipy.linalg.expm(Y)
 
 
+def metric_power(metric, alpha=-0.5, cutoff=1.0e-14):
+    """psi4 Matrix::power(alpha, cutoff) as ``integrals.py:45`` calls it
+    (psi4 unpinned; its published behaviour): eigenvalues below cutoff x the
+    largest magnitude are dropped for negative powers, the rest raised to
+    alpha.  Parity unpinned: psi4 is absent here."""
+    a, V = np.linalg.eigh(metric)
+    amax = max(abs(a[0]), abs(a[-1]))
+    out = np.zeros_like(a)
+    for i, ai in enumerate(a):
+        if alpha < 0.0 and abs(ai) < cutoff * amax:
+            continue
+        v = ai ** alpha
+        out[i] = v if np.isfinite(v) else 0.0
+    return V @ np.diag(out) @ V.T
+
+
+def b_mnl(mnk, metric):
+    """``integrals.py:45-49``: einsum("mnk,kl->mnl", mnk, metric^(-1/2))."""
+    return np.einsum("mnk,kl->mnl", mnk, metric_power(metric), optimize=True)
+
+
+def density_hf(C, j0, j1):
+    """sum_{j0 <= j < j1} C[:, j] C[:, j]^T (``integrals.py:493-510``,
+    computeD_HF with [0, nbeta), computeDalpha_HF with [nbeta, nalpha))."""
+    Cs = C[:, j0:j1]
+    return Cs @ Cs.T
+
+
+def jk_hf_full(D, I):
+    """J = einsum("ls,mnsl->mn"), K = einsum("nl,mnsl->ms") (``integrals.py:528-543``)."""
+    N = D.shape[0]
+    J = (I.reshape(N * N, N * N) @ D.T.reshape(-1)).reshape(N, N)
+    K = np.einsum("nl,mnsl->ms", D, I, optimize=True)
+    return J, K
+
+
 def eri_from_b(b):
     """(mn|sl) = sum_Q b[m, n, Q] b[s, l, Q] (the exact RI identity)."""
     N, _, Q = b.shape

@@ -59,8 +59,16 @@ SIGNATURES = {
     "gb_lagrange_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_energy_elec_workspace_f64": (_Z, [_I, _I]),
     "gb_energy_elec_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_ri_factor_f64": (_I, [_P, _P, _I, _I, _P, _P]),
+    "gb_graph_begin": (_I, [_P]),
+    "gb_graph_end": (_I, [_P, _P]),
+    "gb_graph_launch": (_I, [_P, _P]),
+    "gb_graph_destroy": (_I, [_P]),
+    "gb_density_hf_f64": (_I, [_P, _I, _I, _I, _P, _P]),
+    "gb_jk_hf_full_workspace_f64": (_Z, [_I]),
+    "gb_jk_hf_full_f64": (_I, [_P, _P, _I, _P, _P, _P, _Z, _P]),
     "gb_rotate_orbital_workspace_f64": (_Z, [_I]),
-    "gb_rotate_orbital_f64": (_I, [_P, _P, _I, _I, _P, _P, _Z, _P]),
+    "gb_rotate_orbital_f64": (_I, [_P, _P, _I, _I, _c.c_double, _P, _P, _Z, _P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
     "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
     "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),

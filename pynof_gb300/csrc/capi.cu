@@ -1,6 +1,7 @@
 // Status reporting and small utility entry points of the C ABI.
 #include <cstdarg>
 #include <cstdio>
+#include <new>
 
 #include "gb_common.cuh"
 
@@ -58,3 +59,63 @@ extern "C" int gb_check_symmetric_f64(const double* b, int nbf, int naux, double
   GB_CHECK_LAUNCH("symmetric_diff");
   return GB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Capture of a caller's stream work into a CUDA graph (thread-local mode, so
+// other threads' CUDA calls are not affected while a capture is open).
+// ---------------------------------------------------------------------------
+using gb::clear_error;
+using gb::cuda_status;
+using gb::set_error;
+
+struct gb_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int gb_graph_begin(void* stream) {
+  clear_error();
+  GB_REQUIRE(stream, GB_ERR_INVALID_ARG, "gb_graph_begin: capture needs a non-default stream");
+  return cuda_status(cudaStreamBeginCapture(static_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal),
+                     "cudaStreamBeginCapture");
+}
+
+extern "C" int gb_graph_end(void* stream, gb_graph** out) {
+  clear_error();
+  GB_REQUIRE(stream && out, GB_ERR_INVALID_ARG, "gb_graph_end: null argument");
+  cudaGraph_t g = nullptr;
+  GB_TRY(cuda_status(cudaStreamEndCapture(static_cast<cudaStream_t>(stream), &g), "cudaStreamEndCapture"));
+  cudaGraphExec_t e = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&e, g, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_status(ei, "cudaGraphInstantiate");
+  }
+  gb_graph* h = new (std::nothrow) gb_graph;
+  if (!h) {
+    cudaGraphExecDestroy(e);
+    cudaGraphDestroy(g);
+    set_error(GB_ERR_INVALID_ARG, "gb_graph_end: out of host memory");
+    return GB_ERR_INVALID_ARG;
+  }
+  h->graph = g;
+  h->exec = e;
+  *out = h;
+  return GB_OK;
+}
+
+extern "C" int gb_graph_launch(gb_graph* g, void* stream) {
+  clear_error();
+  GB_REQUIRE(g && g->exec, GB_ERR_INVALID_ARG, "gb_graph_launch: no graph");
+  return cuda_status(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch");
+}
+
+extern "C" int gb_graph_destroy(gb_graph* g) {
+  clear_error();
+  if (!g) return GB_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return GB_OK;
+}
+

@@ -287,3 +287,41 @@ extern "C" int gb_lagrange2_full_f64(const double* C, const double* H, const dou
   }
   return GB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// HF-JK helpers: computeD_HF / computeDalpha_HF and JK_HF_Full_GPU
+// ---------------------------------------------------------------------------
+extern "C" int gb_density_hf_f64(const double* C, int nbf, int j0, int j1, double* D, void* stream) {
+  clear_error();
+  const int N = nbf;
+  GB_REQUIRE(N > 0 && 0 <= j0 && j0 <= j1 && j1 <= N, GB_ERR_BAD_SHAPE,
+             "gb_density_hf_f64: need 0 <= j0 <= j1 <= nbf (nbf=%d j0=%d j1=%d)", N, j0, j1);
+  GB_REQUIRE(C && D, GB_ERR_INVALID_ARG, "gb_density_hf_f64: null pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (j1 == j0) return cuda_status(cudaMemsetAsync(D, 0, sizeof(double) * N * N, s), "cudaMemsetAsync");
+  // D[m][n] = sum_j C[m][j0 + j] C[n][j0 + j]
+  GemmF64 g{};
+  g.M = N; g.N = N; g.K = j1 - j0; g.batch = 1;
+  g.A = {C + j0, 0, lin(N), lin(1)};
+  g.B = {C + j0, 0, lin(1), lin(N)};
+  g.C = {D, 0, lin(N), lin(1)};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_ROWCOL;
+  g.a_kfast = true; g.b_kfast = true;
+  g.tag = "gemm_f64:density";
+  return gemm_f64(g, s);
+}
+
+extern "C" size_t gb_jk_hf_full_workspace_f64(int nbf) {
+  (void)nbf;
+  return 0;
+}
+
+extern "C" int gb_jk_hf_full_f64(const double* D, const double* I, int nbf, double* J, double* K, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  (void)workspace;
+  (void)workspace_bytes;
+  clear_error();
+  GB_TRY(check_full(nbf, 1));
+  GB_REQUIRE(D && I && J && K, GB_ERR_INVALID_ARG, "gb_jk_hf_full_f64: null pointer");
+  return jk_full_core(D, I, nbf, 1, J, K, static_cast<cudaStream_t>(stream));
+}

@@ -609,38 +609,6 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
     if (epi_barrier_any(*abort_flag != 0)) ok = false;
     if (ok) {
       tc_fence_after();
-      // 1) fold the FP32 accumulator into the fixed point and park z in shared
-      //    memory (the stage buffers are idle once every MMA has completed)
-      const int row = q * 32 + lane;
-      long long* Zs = reinterpret_cast<long long*>(smem);
-#pragma unroll
-      for (int h = 0; h < CW / 8; ++h) {
-        uint32_t v[8];
-        if constexpr (KIND == 1) {
-          // every chunk is already in R (fixed point, 31 fraction bits)
-#pragma unroll
-          for (int j = 0; j < 8; ++j) Zs[row * (BN + 1) + cg * CW + h * 8 + j] = R[h * 8 + j];
-          continue;
-        }
-        if (has_inexact && !g.fdrain && cols_live) {
-          tmem_ld8_async(lbase + (uint32_t)(3 * BN + h * 8), v);
-          tmem_wait_ld();
-        } else {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) v[j] = 0u;
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          long long z = R[h * 8 + j];
-          if (!g.fdrain) z = (long long)((unsigned long long)z << a.frac) + split_round(__uint_as_float(v[j]) * upE,
-                                                                                        a.frac, two_frac);
-          Zs[row * (BN + 1) + cg * CW + h * 8 + j] = z;
-        }
-      }
-      epi_barrier_any(false);
-      // 2) assemble FP64 and store; each thread keeps one column (lanes along
-      //    the columns) or one row (lanes along the rows), whichever index is
-      //    unit-stride in the output
       double* Cb = g.C + (long long)bz * g.c_sb;
       const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
       const bool rows_fast = g.c_c.div == 0 && g.c_c.s0 == 1 ? false : (g.c_r.div == 0 && g.c_r.s0 == 1);
@@ -657,8 +625,55 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
           if (mr >= 0) Cb[mr + co] = val;
         }
       };
+      // 1) fold the FP32 accumulator into the fixed point.  When the output's
+      //    unit-stride index is the tile row (the TMEM lane), this layout
+      //    already stores coalesced: convert and store here.  Otherwise park z
+      //    in shared memory (the stage buffers are idle once every MMA has
+      //    completed) for a transposed pass.
+      const int row = q * 32 + lane;
+      long long* Zs = reinterpret_cast<long long*>(smem);
+      // z of this thread's row for its CW columns, handed to sink(c, z)
+      auto fold = [&](auto&& sink) {
+#pragma unroll
+        for (int h = 0; h < CW / 8; ++h) {
+          if constexpr (KIND == 1) {
+            // every chunk is already in R (fixed point, 31 fraction bits)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) sink(cg * CW + h * 8 + j, R[h * 8 + j]);
+          } else {
+            uint32_t v[8];
+            if (has_inexact && !g.fdrain && cols_live) {
+              tmem_ld8_async(lbase + (uint32_t)(3 * BN + h * 8), v);
+              tmem_wait_ld();
+            } else {
+#pragma unroll
+              for (int j = 0; j < 8; ++j) v[j] = 0u;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              long long z = R[h * 8 + j];
+              if (!g.fdrain)
+                z = (long long)((unsigned long long)z << a.frac) +
+                    split_round(__uint_as_float(v[j]) * upE, a.frac, two_frac);
+              sink(cg * CW + h * 8 + j, z);
+            }
+          }
+        }
+      };
+      // (the TMEM loads inside fold are warp-collective: no per-thread branch around it)
+      if (rows_fast) {
+        const bool row_live = row < rlim;
+        fold([&](int c, long long z) {
+          if (row_live && c < clim) put(z, e_srow[row] + e_scol[c], e_roff[row], e_coff[c], e_mr[row], e_mc[c]);
+        });
+      } else {
+        fold([&](int c, long long z) { Zs[row * (BN + 1) + c] = z; });
+      }
+      // 2) rows are not the unit stride: assemble FP64 from shared memory with
+      //    each thread on one column, lanes along the columns
       constexpr int U = 4;  // elements in flight per thread
       if (!rows_fast) {
+        epi_barrier_any(false);
         constexpr int RSTEP = NUM_EPI_WARPS * 32 / BN;
         constexpr int NIT = BM / RSTEP;
         const int c = et % BN, r0 = et / BN;
@@ -684,33 +699,6 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
           } else {
             for (int r = r0; r < rlim; r += RSTEP)
               put(Zs[r * (BN + 1) + c], e_srow[r] + sc, e_roff[r], co, e_mr[r], mc);
-          }
-        }
-      } else {
-        constexpr int CSTEP = NUM_EPI_WARPS * 32 / BM;
-        constexpr int NIT = BN / CSTEP;
-        const int r = et % BM, c0 = et / BM;
-        if (r < rlim) {
-          const int sr = e_srow[r];
-          const long long ro = e_roff[r], mr = e_mr[r];
-          if (clim == BN && NIT % U == 0) {
-#pragma unroll 1
-            for (int it = 0; it < NIT; it += U) {
-              long long zv[U], co[U], mc[U];
-              int sc[U];
-#pragma unroll
-              for (int u = 0; u < U; ++u) {
-                const int c = c0 + (it + u) * CSTEP;
-                zv[u] = Zs[r * (BN + 1) + c];
-                sc[u] = e_scol[c];
-                co[u] = e_coff[c];
-                mc[u] = g.sym == SYM_NONE ? -1 : e_mc[c];
-              }
-#pragma unroll
-              for (int u = 0; u < U; ++u) put(zv[u], sr + sc[u], ro, co[u], mr, mc[u]);
-            }
-          } else {
-            for (int c = c0; c < clim; c += CSTEP) put(Zs[r * (BN + 1) + c], sr + e_scol[c], ro, e_coff[c], mr, e_mc[c]);
           }
         }
       }

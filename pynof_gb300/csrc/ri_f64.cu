@@ -304,3 +304,26 @@ extern "C" int gb_lagrange2_ri_f64(const double* C, const double* H, const doubl
   GB_TRY(launch_lagrange2_finish(bMO, w, Hmat, n, elag, N, P, Q, s));
   return GB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// b_mnl = sum_k (mn|k) M[k][l]  (compute_integrals, integrals.py:35-49: the
+// einsum "mnk,kl->mnl" with M = metric^(-1/2)); M symmetric.  (mn|k) is
+// symmetric in (m, n), so only the rows m <= n are computed and mirrored.
+// ---------------------------------------------------------------------------
+extern "C" int gb_ri_factor_f64(const double* mnk, const double* M, int nbf, int naux, double* b, void* stream) {
+  clear_error();
+  const int N = nbf, Q = naux;
+  GB_REQUIRE(N > 0 && Q > 0, GB_ERR_BAD_SHAPE, "gb_ri_factor_f64: bad sizes nbf=%d naux=%d", N, Q);
+  GB_REQUIRE((long long)N * N <= 2147483647LL, GB_ERR_BAD_SHAPE, "gb_ri_factor_f64: nbf=%d too large", N);
+  GB_REQUIRE(mnk && M && b, GB_ERR_INVALID_ARG, "gb_ri_factor_f64: null pointer");
+  GemmF64 g{};
+  g.M = N * N; g.N = Q; g.K = Q; g.batch = 1;
+  g.A = {mnk, 0, lin(Q), lin(1)};  // A((m,n), k) = mnk[(m,n)][k]
+  g.B = {M, 0, lin(Q), lin(1)};    // B(k, l) = M[k][l]
+  g.C = {b, 0, lin(Q), lin(1)};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_NONE;
+  g.a_kfast = true; g.b_kfast = false;
+  g.tag = "gemm_f64:ri_factor";
+  return gemm_f64(g, static_cast<cudaStream_t>(stream));
+}
+

@@ -99,8 +99,8 @@ extern "C" size_t gb_rotate_orbital_workspace_f64(int nbf) {
   return c.used;
 }
 
-extern "C" int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double* Cout,
-                                     void* workspace, size_t workspace_bytes, void* stream) {
+extern "C" int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double norm1,
+                                     double* Cout, void* workspace, size_t workspace_bytes, void* stream) {
   clear_error();
   const int N = nbf, P = nbf5;
   GB_REQUIRE(N > 0 && P > 0 && P <= N, GB_ERR_BAD_SHAPE, "gb_rotate_orbital_f64: need 0 < nbf5 <= nbf");
@@ -117,13 +117,16 @@ extern "C" int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, 
   const long long NN = (long long)N * N;
 
   GB_LAUNCH("rotate_build", s, build_antisym_kernel<<<cdiv(NN, 256), 256, 0, s>>>(y, N, P, Y));
-  GB_TRY(cuda_status(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), s), "cudaMemsetAsync"));
-  GB_LAUNCH("rotate_norm", s, col_abs_max_kernel<<<cdiv(N, 128), 128, 0, s>>>(Y, N, dnorm));
-  unsigned long long nbits = 0;
-  GB_TRY(cuda_status(cudaMemcpyAsync(&nbits, dnorm, sizeof(nbits), cudaMemcpyDeviceToHost, s), "norm copy"));
-  GB_TRY(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
-  double norm;
-  memcpy(&norm, &nbits, sizeof(norm));
+  double norm = norm1;
+  if (!(norm1 >= 0.0)) {
+    // no bound from the caller: measure ||Y||_1 on the device (one synchronisation)
+    GB_TRY(cuda_status(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), s), "cudaMemsetAsync"));
+    GB_LAUNCH("rotate_norm", s, col_abs_max_kernel<<<cdiv(N, 128), 128, 0, s>>>(Y, N, dnorm));
+    unsigned long long nbits = 0;
+    GB_TRY(cuda_status(cudaMemcpyAsync(&nbits, dnorm, sizeof(nbits), cudaMemcpyDeviceToHost, s), "norm copy"));
+    GB_TRY(cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
+    memcpy(&norm, &nbits, sizeof(norm));
+  }
   GB_REQUIRE(std::isfinite(norm), GB_ERR_NONFINITE, "gb_rotate_orbital_f64: step y is not finite");
   GB_REQUIRE(norm < 0x1p60, GB_ERR_INVALID_ARG, "gb_rotate_orbital_f64: step norm %g too large", norm);
   int sq = 0;

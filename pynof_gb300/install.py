@@ -10,7 +10,7 @@ unchanged.  The dispatchers keep the reference's CPU branches for
 """
 from __future__ import annotations
 
-from . import integrals, integrals_full, utils
+from . import integrals, integrals_full, integrals_hf, utils
 
 #: (module attribute path in pynof, replacement) for the p.gpu branches
 GPU_FUNCTIONS = {
@@ -21,6 +21,8 @@ GPU_FUNCTIONS = {
     "integrals.Integrals_MO_RI_GPU": integrals.Integrals_MO_RI_GPU,
     "integrals.Integrals_MO_Full_GPU": integrals_full.Integrals_MO_Full_GPU,
     "utils.computeF_RC_GPU": utils.computeF_RC_GPU,
+    "integrals.JK_HF_Full_GPU": integrals_hf.JK_HF_Full_GPU,
+    "integrals.JKalpha_HF_Full_GPU": integrals_hf.JKalpha_HF_Full_GPU,
 }
 
 
@@ -72,13 +74,18 @@ def install(pynof) -> dict:
     # so they are replaced whole; the reference CPU branch stays behind p.gpu=False
     # rotate_orbital (utils.py:550-565) runs scipy expm on the host: on the
     # device path it becomes the FP64 device rotation
-    for name, gpu_fn in (("computeLagrange2", utils.computeLagrange2), ("ENERGY1r", utils.ENERGY1r),
-                         ("rotate_orbital", utils.rotate_orbital)):
-        cpu_fn = getattr(pynof.utils, name)
-        saved["utils." + name] = cpu_fn
-        saved["pynof." + name] = getattr(pynof, name)
+    for modname, name, gpu_fn in (("utils", "computeLagrange2", utils.computeLagrange2),
+                                  ("utils", "ENERGY1r", utils.ENERGY1r),
+                                  ("utils", "rotate_orbital", utils.rotate_orbital),
+                                  # cupy inline (integrals.py:493-510)
+                                  ("integrals", "computeD_HF", integrals_hf.computeD_HF),
+                                  ("integrals", "computeDalpha_HF", integrals_hf.computeDalpha_HF)):
+        mod = getattr(pynof, modname)
+        cpu_fn = getattr(mod, name)
+        saved[modname + "." + name] = cpu_fn
+        saved["pynof." + name] = getattr(pynof, name, cpu_fn)
         disp = _gpu_or_cpu(gpu_fn, cpu_fn)
-        setattr(pynof.utils, name, disp)
+        setattr(mod, name, disp)
         setattr(pynof, name, disp)
     return saved
 

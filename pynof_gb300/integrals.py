@@ -164,3 +164,34 @@ def JKH_MO_tmp(C, H, I, b_mnl, p):
     from . import integrals_full
 
     return integrals_full.Integrals_MO_Full_GPU(C, H, I, p)
+
+
+# ---------------------------------------------------------------------------
+# The RI factor itself (compute_integrals, integrals.py:35-49)
+# ---------------------------------------------------------------------------
+def metric_power(metric, alpha: float = -0.5, cutoff: float = 1.0e-14):
+    """The metric power compute_integrals takes from psi4
+    (``metric.power(-0.5, 1.0e-14)``, ``integrals.py:45``; psi4 is a conda
+    dependency the reference does not pin): eigendecomposition of the
+    symmetric metric; for a negative power, eigenvalues whose magnitude is
+    below ``cutoff`` times the largest are dropped (their power is zero), the
+    others are raised to ``alpha``.  Host FP64 (LAPACK), as the north-star
+    keeps the metric inverse square root in FP64."""
+    a, V = np.linalg.eigh(np.asarray(metric, dtype=np.float64))
+    amax = max(abs(a[0]), abs(a[-1])) if a.size else 0.0
+    keep = ~((alpha < 0.0) & (np.abs(a) < cutoff * amax))
+    pw = np.zeros_like(a)
+    with np.errstate(all="ignore"):
+        pw[keep] = np.power(a[keep], alpha)
+    pw[~np.isfinite(pw)] = 0.0
+    return (V * pw) @ V.T
+
+
+def compute_b_mnl(mnk, metric, nslices: int | None = None, metric_is_power: bool = False):
+    """b_mnl = einsum("mnk,kl->mnl", mnk, metric^(-1/2)) (``integrals.py:41-49``)
+    with the three-centre integrals mnk (nbf, nbf, naux) as psi4 returns them
+    (squeezed): the metric power on the host, the contraction on the device
+    (FP64 DMMA, or the split-product tensor-core GEMM with ``nslices``).
+    Returns the device tensor (resident, as ``cp.array(b_mnl)`` at ``:53``)."""
+    M = np.asarray(metric, dtype=np.float64) if metric_is_power else metric_power(metric)
+    return ops.ri_factor(as_device(mnk), as_device(M), nslices)

@@ -12,6 +12,8 @@ Closed shell (MSpin == 0) is the supported case, as on the device path.
 """
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 import scipy.linalg
 
@@ -182,12 +184,19 @@ def calcoccg(gamma, J_MO, K_MO, H_core, p):
     return g
 
 
+@functools.lru_cache(maxsize=64)
+def _packed_index(nbf: int, nbf5: int):
+    """Flat indices of (i, j > i), i < nbf5, row-major: the packed order of y."""
+    iu, ju = np.triu_indices(nbf, 1)
+    keep = iu < nbf5
+    return iu[keep] * nbf + ju[keep], ju[keep] * nbf + iu[keep]
+
+
 def orbital_gradient(elag, p):
     """Packed 4 (elag - elag^T) over i < nbf5, j > i (``pnof.py:1114-1131``)."""
-    g = 4.0 * (elag - elag.T)
-    iu, ju = np.triu_indices(p.nbf, 1)
-    keep = iu < p.nbf5
-    return g[iu[keep], ju[keep]]
+    ij, ji = _packed_index(p.nbf, p.nbf5)
+    e = np.asarray(elag).reshape(-1)
+    return 4.0 * (e[ij] - e[ji])
 
 
 def rotate_orbital(y, C, p):

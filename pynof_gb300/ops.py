@@ -8,6 +8,7 @@ CUDA tensors (``to_device`` converts numpy arrays).
 """
 from __future__ import annotations
 
+import ctypes
 import threading
 
 import numpy as np
@@ -103,16 +104,23 @@ def jkj_ri(C: torch.Tensor, b: torch.Tensor, nbf5: int):
     return J, K
 
 
-def jkh_mo_ri(C: torch.Tensor, H: torch.Tensor, b: torch.Tensor, nbf5: int):
+def _outs(out, shapes, dev):
+    """Caller-provided output tensors (checked) or new ones."""
+    if out is None:
+        return [torch.empty(sh, dtype=_F64, device=dev) for sh in shapes]
+    for t, sh in zip(out, shapes):
+        _require(t, sh, "out")
+    return list(out)
+
+
+def jkh_mo_ri(C: torch.Tensor, H: torch.Tensor, b: torch.Tensor, nbf5: int, out=None):
     """J_MO, K_MO (nbf5, nbf5), H_core (nbf5,) from the RI factor (A3)."""
     N, _, Q = b.shape
     _require(C, (N, N), "C")
     _require(H, (N, N), "H")
     _require(b, (N, N, Q), "b")
     dev = b.device
-    J_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
-    K_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
-    H_core = torch.empty((nbf5,), dtype=_F64, device=dev)
+    J_MO, K_MO, H_core = _outs(out, [(nbf5, nbf5), (nbf5, nbf5), (nbf5,)], dev)
     wp, wn = _ws("gb_jkh_mo_ri_workspace_f64", N, nbf5, Q, device=dev)
     _lib.call("gb_jkh_mo_ri_f64", _ptr(C), _ptr(H), _ptr(b), N, nbf5, Q, _ptr(J_MO), _ptr(K_MO), _ptr(H_core),
               wp, wn, _stream(dev))
@@ -133,7 +141,7 @@ def mo_ri(C: torch.Tensor, H: torch.Tensor, b: torch.Tensor, nbf5: int):
     return Hmat, bMO
 
 
-def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
+def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int, out=None):
     """elag (nbf, nbf) and Hmat (nbf, nbf5) (A5, computeLagrange2 RI closed shell).
 
     The diagonals of cj12 / ck12 are ignored (treated as zero)."""
@@ -145,8 +153,7 @@ def lagrange2_ri(C, H, b, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
     _require(cj12, (nbf5, nbf5), "cj12")
     _require(ck12, (nbf5, nbf5), "ck12")
     dev = b.device
-    elag = torch.empty((N, N), dtype=_F64, device=dev)
-    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    elag, Hmat = _outs(out, [(N, N), (N, nbf5)], dev)
     wp, wn = _ws("gb_lagrange2_ri_workspace_f64", N, nbf5, Q, device=dev)
     _lib.call("gb_lagrange2_ri_f64", _ptr(C), _ptr(H), _ptr(b), _ptr(n), _ptr(cj12), _ptr(ck12), N, nbf5, Q,
               nbeta, nalpha, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
@@ -265,18 +272,104 @@ def energy_elec(elag, C, H, n, nbeta: int, nalpha: int, high_spin: bool = False)
     return E
 
 
-def rotate_orbital(y: torch.Tensor, C: torch.Tensor, nbf5: int) -> torch.Tensor:
+def ri_factor(mnk: torch.Tensor, M: torch.Tensor, nslices: int | None = None) -> torch.Tensor:
+    """b[m][n][l] = sum_k mnk[m][n][k] M[k][l] (M symmetric): FP64 DMMA, or the
+    split-product tensor-core GEMM when ``nslices`` is given."""
+    N, N2, Q = mnk.shape
+    if N2 != N:
+        raise ValueError("mnk must be (nbf, nbf, naux)")
+    _require(mnk, (N, N, Q), "mnk")
+    _require(M, (Q, Q), "M")
+    if nslices is not None:
+        return dgemm_mixed(mnk.view(N * N, Q), M, nslices).view(N, N, Q)
+    b = torch.empty((N, N, Q), dtype=_F64, device=mnk.device)
+    _lib.call("gb_ri_factor_f64", _ptr(mnk), _ptr(M), N, Q, _ptr(b), _stream(mnk.device))
+    return b
+
+
+def density_hf(C: torch.Tensor, j0: int, j1: int) -> torch.Tensor:
+    """D = sum_{j0 <= j < j1} C[:, j] C[:, j]^T (computeD_HF / computeDalpha_HF)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    D = torch.empty((N, N), dtype=_F64, device=C.device)
+    _lib.call("gb_density_hf_f64", _ptr(C), N, int(j0), int(j1), _ptr(D), _stream(C.device))
+    return D
+
+
+def jk_hf_full(D: torch.Tensor, I: torch.Tensor):
+    """J, K of one symmetric density from the 4-index tensor (JK_HF_Full_GPU)."""
+    N = D.shape[0]
+    _require(D, (N, N), "D")
+    _require(I, (N, N, N, N), "I")
+    J = torch.empty((N, N), dtype=_F64, device=D.device)
+    K = torch.empty((N, N), dtype=_F64, device=D.device)
+    wp, wn = _ws("gb_jk_hf_full_workspace_f64", N, device=D.device)
+    _lib.call("gb_jk_hf_full_f64", _ptr(D), _ptr(I), N, _ptr(J), _ptr(K), wp, wn, _stream(D.device))
+    return J, K
+
+
+def rotate_orbital(y: torch.Tensor, C: torch.Tensor, nbf5: int, out: torch.Tensor | None = None,
+                   norm1: float = -1.0) -> torch.Tensor:
     """C expm(Y) (rotate_orbital) with Y the antisymmetric matrix of the packed
-    step y (rows i < nbf5 of the strict upper triangle, row-major)."""
+    step y (rows i < nbf5 of the strict upper triangle, row-major).
+
+    norm1: an upper bound of ||Y||_1 (see :func:`antisym_norm1`); negative
+    means "measure it on the device" (one stream synchronisation)."""
     N = C.shape[0]
     _require(C, (N, N), "C")
     nvar = N * (N - 1) // 2 - (N - nbf5) * (N - nbf5 - 1) // 2
     _require(y, (nvar,), "y")
     dev = C.device
-    out = torch.empty_like(C)
+    if out is None:
+        out = torch.empty_like(C)
+    else:
+        _require(out, (N, N), "out")
     wp, wn = _ws("gb_rotate_orbital_workspace_f64", N, device=dev)
-    _lib.call("gb_rotate_orbital_f64", _ptr(y), _ptr(C), N, nbf5, _ptr(out), wp, wn, _stream(dev))
+    _lib.call("gb_rotate_orbital_f64", _ptr(y), _ptr(C), N, nbf5, float(norm1), _ptr(out), wp, wn, _stream(dev))
     return out
+
+
+class StreamGraph:
+    """Work issued by this thread on ``stream`` between ``begin`` and ``end``,
+    captured (thread-local mode) into a CUDA graph and replayed by
+    ``launch``.  The captured work must not allocate or synchronise: give the
+    ops preallocated outputs and grow their workspaces in a run beforehand."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self.handle = ctypes.c_void_p()
+
+    def begin(self):
+        _lib.call("gb_graph_begin", self.stream.cuda_stream)
+
+    def end(self):
+        _lib.call("gb_graph_end", self.stream.cuda_stream, ctypes.byref(self.handle))
+
+    def launch(self):
+        _lib.call("gb_graph_launch", self.handle, self.stream.cuda_stream)
+
+    def __del__(self):
+        if self.handle:
+            try:
+                _lib.call("gb_graph_destroy", self.handle)
+            except Exception:  # interpreter shutdown
+                pass
+            self.handle = ctypes.c_void_p()
+
+
+class AntisymNorm:
+    """||Y||_1 (max column sum of |Y|) of the antisymmetric matrix of a packed
+    step, on the host from y alone (index arrays built once per size)."""
+
+    def __init__(self, nbf: int, nbf5: int):
+        iu, ju = np.triu_indices(nbf, 1)
+        keep = iu < nbf5
+        self.iu, self.ju, self.n = iu[keep], ju[keep], nbf
+
+    def __call__(self, y) -> float:
+        a = np.abs(np.asarray(y, dtype=np.float64))
+        col = np.bincount(self.iu, a, minlength=self.n) + np.bincount(self.ju, a, minlength=self.n)
+        return float(col.max()) if col.size else 0.0
 
 
 # ----------------------------------------------------------------------------
@@ -337,22 +430,20 @@ def jkj_ri_mixed(C: torch.Tensor, prep: PreparedRI, nbf5: int):
     return J, K
 
 
-def jkh_mo_ri_mixed(C, H, prep: PreparedRI, nbf5: int):
+def jkh_mo_ri_mixed(C, H, prep: PreparedRI, nbf5: int, out=None):
     """J_MO, K_MO, H_core on the tensor cores (A3)."""
     N, Q, S = prep.nbf, prep.naux, prep.nslices
     _require(C, (N, N), "C")
     _require(H, (N, N), "H")
     dev = prep.device
-    J_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
-    K_MO = torch.empty((nbf5, nbf5), dtype=_F64, device=dev)
-    H_core = torch.empty((nbf5,), dtype=_F64, device=dev)
+    J_MO, K_MO, H_core = _outs(out, [(nbf5, nbf5), (nbf5, nbf5), (nbf5,)], dev)
     wp, wn = _ws("gb_jkh_mo_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
     _lib.call("gb_jkh_mo_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J_MO), _ptr(K_MO),
               _ptr(H_core), wp, wn, _stream(dev))
     return J_MO, K_MO, H_core
 
 
-def lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int):
+def lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int, out=None):
     """elag, Hmat on the tensor cores (A5, closed shell)."""
     N, Q, S = prep.nbf, prep.naux, prep.nslices
     _require(C, (N, N), "C")
@@ -361,8 +452,7 @@ def lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: 
     _require(cj12, (nbf5, nbf5), "cj12")
     _require(ck12, (nbf5, nbf5), "ck12")
     dev = prep.device
-    elag = torch.empty((N, N), dtype=_F64, device=dev)
-    Hmat = torch.empty((N, nbf5), dtype=_F64, device=dev)
+    elag, Hmat = _outs(out, [(N, N), (N, nbf5)], dev)
     wp, wn = _ws("gb_lagrange2_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
     _lib.call("gb_lagrange2_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), _ptr(n), _ptr(cj12), _ptr(ck12), N,
               nbf5, Q, nbeta, nalpha, S, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))

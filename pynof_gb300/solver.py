@@ -29,10 +29,21 @@ from . import integrals, nof, ops
 class Backend:
     """Device contractions for one molecule.
 
-    precision: "fp64" (DMMA) or "mixed" (tcgen05 digit slices, ``nslices``)."""
+    precision: "fp64" (DMMA) or "mixed" (tcgen05 digit slices, ``nslices``).
 
-    def __init__(self, st, b, H, precision: str = "mixed", nslices: int = 6, device=None, stream=None):
+    The orbital steps of the AMSgrad loop keep C resident on the device
+    (``orbital_begin`` / ``orbital_step`` / ``keep_best`` / ``best_C``).  With
+    ``use_graphs`` each step -- rotation C expm(Y), computeJKH_MO and
+    computeLagrange2 at the new orbitals -- is one CUDA-graph replay, captured
+    once per (precision, number of expm squarings)."""
+
+    def __init__(self, st, b, H, precision: str = "mixed", nslices: int = 6, device=None, stream=None,
+                 use_graphs: bool = True):
         self.st = st
+        self.use_graphs = use_graphs
+        self._norm = ops.AntisymNorm(st.nbf, st.nbf5)
+        self._graphs: dict = {}
+        self._buf: dict | None = None
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.stream = stream if stream is not None else torch.cuda.Stream(self.device)
         self.precision = precision
@@ -46,6 +57,7 @@ class Backend:
     def set_precision(self, precision: str, nslices: int | None = None):
         """Switch arithmetic (e.g. to FP64 near convergence)."""
         self.precision = precision
+        self._graphs.clear()  # the new path may need a larger workspace: recapture
         if nslices is not None and nslices != self.nslices:
             self.nslices = nslices
             self.prep = None
@@ -64,34 +76,116 @@ class Backend:
             out = [t.to("cpu", non_blocking=False) for t in ts]
         return [o.numpy() for o in out]
 
-    def jkh_mo(self, C):
+    # device-side pieces (current stream = self.stream)
+    def _jkh_mo_dev(self, dC):
         self.calls["jkh_mo"] += 1
-        P = self.st.nbf5
-        with torch.cuda.stream(self.stream):
-            dC = ops.to_device(C, self.device)
-            if self.precision == "mixed":
-                res = ops.jkh_mo_ri_mixed(dC, self.H, self.prep, P)
-            else:
-                res = ops.jkh_mo_ri(dC, self.H, self.b, P)
-            return self._sync_host(*res)
+        if self.precision == "mixed":
+            return ops.jkh_mo_ri_mixed(dC, self.H, self.prep, self.st.nbf5)
+        return ops.jkh_mo_ri(dC, self.H, self.b, self.st.nbf5)
 
-    def rotate(self, y, C):
-        """C expm(Y) on the device (FP64), host in / host out."""
-        with torch.cuda.stream(self.stream):
-            out = ops.rotate_orbital(ops.to_device(y, self.device), ops.to_device(C, self.device), self.st.nbf5)
-            return self._sync_host(out)[0]
-
-    def lagrange2(self, C, n, cj12, ck12):
+    def _lagrange2_dev(self, dC, dn, dcj, dck):
         self.calls["lagrange2"] += 1
         st = self.st
+        if self.precision == "mixed":
+            return ops.lagrange2_ri_mixed(dC, self.H, self.prep, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
+        return ops.lagrange2_ri(dC, self.H, self.b, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
+
+    def jkh_mo(self, C):
         with torch.cuda.stream(self.stream):
-            dC = ops.to_device(C, self.device)
-            dn, dcj, dck = (ops.to_device(x, self.device) for x in (n, cj12, ck12))
-            if self.precision == "mixed":
-                res = ops.lagrange2_ri_mixed(dC, self.H, self.prep, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
+            return self._sync_host(*self._jkh_mo_dev(ops.to_device(C, self.device)))
+
+    # ---- device-resident orbital steps ---------------------------------
+    def _static(self):
+        if self._buf is None:
+            N, P, nvar = self.st.nbf, self.st.nbf5, self.st.nvar
+
+            def z(*shape):
+                return torch.zeros(shape, dtype=torch.float64, device=self.device)
+
+            self._buf = {"C": z(N, N), "Cprev": z(N, N), "best": z(N, N), "y": z(nvar), "n": z(P), "cj": z(P, P),
+                         "ck": z(P, P), "J": z(P, P), "K": z(P, P), "Hc": z(P), "elag": z(N, N), "Hmat": z(N, P)}
+        return self._buf
+
+    def _step_body(self, sq):
+        """Rotation by the static y with sq squarings (none when sq < 0), then
+        the two contractions at the static C into the static outputs.  Issues
+        launches only (no allocation, no synchronisation)."""
+        b, st = self._static(), self.st
+        if sq >= 0:
+            b["Cprev"].copy_(b["C"])
+            ops.rotate_orbital(b["y"], b["Cprev"], st.nbf5, out=b["C"], norm1=0.5 * 2.0 ** sq)
+        self.calls["jkh_mo"] += 1
+        self.calls["lagrange2"] += 1
+        mo_out, l2_out = (b["J"], b["K"], b["Hc"]), (b["elag"], b["Hmat"])
+        if self.precision == "mixed":
+            ops.jkh_mo_ri_mixed(b["C"], self.H, self.prep, st.nbf5, out=mo_out)
+            ops.lagrange2_ri_mixed(b["C"], self.H, self.prep, b["n"], b["cj"], b["ck"], st.nbf5, st.nbeta,
+                                   st.nalpha, out=l2_out)
+        else:
+            ops.jkh_mo_ri(b["C"], self.H, self.b, st.nbf5, out=mo_out)
+            ops.lagrange2_ri(b["C"], self.H, self.b, b["n"], b["cj"], b["ck"], st.nbf5, st.nbeta, st.nalpha,
+                             out=l2_out)
+
+    def _run_step(self, sq):
+        b = self._static()
+        with torch.cuda.stream(self.stream):
+            if not self.use_graphs:
+                self._step_body(sq)
             else:
-                res = ops.lagrange2_ri(dC, self.H, self.b, dn, dcj, dck, st.nbf5, st.nbeta, st.nalpha)
-            return self._sync_host(*res)
+                key = (self.precision, self.nslices, sq)
+                g = self._graphs.get(key)
+                if g is None:
+                    # grow the workspaces in a plain run on a copy of the state,
+                    # then capture (thread-local mode: other requests' threads
+                    # keep running)
+                    saved = b["C"].clone()
+                    self._step_body(sq)
+                    b["C"].copy_(saved)
+                    g = ops.StreamGraph(self.stream)
+                    g.begin()
+                    try:
+                        self._step_body(sq)
+                    finally:
+                        g.end()
+                    self._graphs[key] = g
+                g.launch()
+            return self._sync_host(b["J"], b["K"], b["Hc"], b["elag"])
+
+    def orbital_begin(self, C, n, cj12, ck12):
+        """Load C, n, cj12, ck12 (diagonals already zero) and return host
+        (J_MO, K_MO, H_core, elag) at C."""
+        b = self._static()
+        with torch.cuda.stream(self.stream):
+            for k, x in (("C", C), ("n", n), ("cj", cj12), ("ck", ck12)):
+                b[k].copy_(torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)))
+            b["best"].copy_(b["C"])
+        return tuple(self._run_step(-1))
+
+    def orbital_step(self, y):
+        """C <- C expm(Y(y)) on the device; host (J_MO, K_MO, H_core, elag) at the new C."""
+        b = self._static()
+        nrm = self._norm(y)
+        if not np.isfinite(nrm):
+            raise FloatingPointError("orbital step is not finite")
+        sq = 0
+        while nrm > 0.5:
+            nrm *= 0.5
+            sq += 1
+        with torch.cuda.stream(self.stream):
+            b["y"].copy_(torch.from_numpy(np.ascontiguousarray(y, dtype=np.float64)))
+        return tuple(self._run_step(sq))
+
+    def keep_best(self):
+        with torch.cuda.stream(self.stream):
+            self._static()["best"].copy_(self._static()["C"])
+
+    def best_C(self):
+        return self._sync_host(self._static()["best"])[0]
+
+    def lagrange2(self, C, n, cj12, ck12):
+        with torch.cuda.stream(self.stream):
+            dn, dcj, dck = (ops.to_device(x, self.device) for x in (n, cj12, ck12))
+            return self._sync_host(*self._lagrange2_dev(ops.to_device(C, self.device), dn, dcj, dck))
 
 
 @dataclasses.dataclass
@@ -136,8 +230,13 @@ def orbopt_adam(gamma, C, be, p, state: SolveState):
     """``minimization.py:200-253``: AMSgrad steps of orbital rotations."""
     n, _ = nof.ocupacion_softmax(gamma, p)
     cj12, ck12 = nof.cjckd8(n, p)
-    y0 = np.zeros(p.nvar)
-    E = calcorbe(y0, n, cj12, ck12, C, be, p)
+    np.fill_diagonal(cj12, 0.0)  # as calce / calcorbg do in place
+    np.fill_diagonal(ck12, 0.0)
+    # C stays on the device for the whole loop: E (calcorbe) and the gradient
+    # (calcorbg) at the same orbitals come from one device round trip, and so
+    # do the rotation plus both contractions after each step
+    J_MO, K_MO, H_core, elag = be.orbital_begin(C, n, cj12, ck12)
+    E = nof.calce(n, cj12, ck12, J_MO, K_MO, H_core, p)
     alpha, beta1, beta2 = state.alpha, 0.7, 0.999
     m = np.zeros(p.nvar)
     v = np.zeros(p.nvar)
@@ -147,7 +246,7 @@ def orbopt_adam(gamma, C, be, p, state: SolveState):
     nit = 0
     for i in range(state.maxloop):
         nit += 1
-        grad = calcorbg(y0, n, cj12, ck12, C, be, p)
+        grad = nof.orbital_gradient(elag, p)
         if np.linalg.norm(grad) < 1e-4 and improved:
             success = True
             break
@@ -157,11 +256,14 @@ def orbopt_adam(gamma, C, be, p, state: SolveState):
         vhat = v / (1.0 - beta2 ** (i + 1))
         vhat_max = np.maximum(vhat_max, vhat)
         y = -alpha * mhat / np.sqrt(vhat_max + 1e-8)
-        C = be.rotate(y, C)
-        E = calcorbe(y0, n, cj12, ck12, C, be, p)
+        J_MO, K_MO, H_core, elag = be.orbital_step(y)
+        E = nof.calce(n, cj12, ck12, J_MO, K_MO, H_core, p)
         if E < best_E:
-            best_C, best_E = C, E
+            be.keep_best()
+            best_E = E
             improved = True
+    if improved:
+        best_C = be.best_C()
     if not improved:
         state.alpha /= 10
         state.maxloop += 30

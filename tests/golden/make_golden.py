@@ -217,6 +217,22 @@ def run_case(pynof, name, workload, seed, full, jit):
             checks["JKj_Full_jit_vs_numpy"] = max(nrel(Jj, Jf), nrel(Kj, Kf))
             a2, b2, c2 = pynof.JKH_MO_Full_jit(C, H, I, st.nbf, P)
             checks["JKH_MO_Full_jit_vs_numpy"] = max(nrel(a2, a), nrel(b2, bb))
+        # HF-JK helpers (integrals.py:490-560): closed-shell density and its
+        # J, K; the singly-occupied density and its J, K with two open shells
+        D_hf = pynof.computeD_HF(C, pf)
+        J_hf, K_hf = pynof.computeJK_HF(D_hf, I, [], pf)
+        pa = make_param(st, RI=False, nsoc=2, nalpha=st.nbeta + 2)
+        # JKalpha_HF_Full_GPU (integrals.py:557-562) = computeDalpha_HF's einsum
+        # then JK_HF_Full's einsums; the CPU route (JKalpha_HF_Full_jit) loops
+        # over nu < mu only and leaves the diagonals of D, J and K at zero
+        Da_hf = pynof.computeDalpha_HF(C, pa)
+        Ja_hf, Ka_hf = pynof.JK_HF_Full_jit(Da_hf, I, pa.nbeta, pa.nbf, pa.nbf5)
+        Dj, Jj, Kj = pynof.computeJKalpha_HF(C, I, [], pa)
+        off = ~np.eye(st.nbf, dtype=bool)
+        checks["JKalpha_HF_jit_D_offdiag_vs_einsum"] = nrel(Dj[off], Da_hf[off])
+        checks["JKalpha_HF_jit_D_J_diagonal_max"] = float(max(np.abs(np.diag(Dj)).max(), np.abs(np.diag(Jj)).max()))
+        checks["JKalpha_HF_jit_J_vs_gpu_route"] = nrel(Jj, Ja_hf)  # differs: D's diagonal is missing
+        out.update(D_hf=D_hf, J_hf=J_hf, K_hf=K_hf, Da_hf=Da_hf, Ja_hf=Ja_hf, Ka_hf=Ka_hf)
 
     meta = dict(case=name, workload=workload, seed=seed, sizes=synthetic.WORKLOADS[workload],
                 numpy=np.__version__, checks=checks)

@@ -105,3 +105,26 @@ def test_energy1r_both_routes(case):
             assert nrel(elagh, g["elag1r_hf"]) < TOL, mode
         finally:
             integrals.set_precision("mixed", 6)
+
+
+@pytest.mark.parametrize("name", ["c1", "water"])
+def test_hf_jk_golden(torch_cuda, name):
+    """The HF-JK drop-ins against the reference's own outputs."""
+    import types as _t
+
+    from pynof_gb300 import integrals, integrals_hf
+
+    g = load_golden(name)
+    p = param_for(GOLDEN_CASES[name])
+    I = integrals.upload_integrals(np.einsum("mnQ,slQ->mnsl", g["b"], g["b"]), None)[0]
+    D = integrals_hf.computeD_HF(g["C"], p)
+    assert nrel(D, g["D_hf"]) < 1e-12
+    J, K = integrals_hf.computeJK_HF(D, I, None, p)
+    assert nrel(J, g["J_hf"]) < 1e-10 and nrel(K, g["K_hf"]) < 1e-10
+    pa = _t.SimpleNamespace(**vars(p))
+    pa.nalpha = p.nbeta + 2
+    Da, Ja, Ka = integrals_hf.computeJKalpha_HF(g["C"], I, None, pa)
+    assert nrel(Da, g["Da_hf"]) < 1e-12
+    assert nrel(Ja, g["Ja_hf"]) < 1e-10 and nrel(Ka, g["Ka_hf"]) < 1e-10
+    assert nrel(integrals_hf.computeDalpha_HF(g["C"], pa), g["Da_hf"]) < 1e-12
+

@@ -81,3 +81,18 @@ def test_rotate_rejects_bad_input(torch_cuda):
         ops.rotate_orbital(y, C, P)
     with pytest.raises(ValueError):
         ops.rotate_orbital(ops.to_device(np.zeros(3)), C, P)
+
+
+def test_host_norm_bound_matches_device_norm(torch_cuda):
+    """A caller-supplied ||Y||_1 (no synchronisation) picks the same number of
+    squarings as the device measurement: bitwise-identical results."""
+    from pynof_gb300 import ops
+
+    N, P = 80, 40
+    rng = np.random.default_rng(5)
+    y = rng.standard_normal(_nvar(N, P)) * 0.4
+    C, _ = np.linalg.qr(rng.standard_normal((N, N)))
+    dy, dC = ops.to_device(y), ops.to_device(C)
+    a = ops.rotate_orbital(dy, dC, P).cpu().numpy()
+    b = ops.rotate_orbital(dy, dC, P, norm1=ops.AntisymNorm(N, P)(y)).cpu().numpy()
+    assert np.array_equal(a, b)

@@ -20,7 +20,7 @@ def test_alone_equals_in_mix(torch_cuda):
     reqs = serve.poisson_stream(6, rate=200.0, nbf_lo=24, nbf_hi=48, seed=5)
     mixed = serve.Server(slots=4, tol=1e-4, maxit=60)
     rep = mixed.run(reqs)
-    assert rep["completed"] == 6 and rep["failed"] == 0
+    assert rep["completed"] == 6 and rep["failed"] == 0, mixed.errors
     assert rep["peak_active"] > 1  # requests were on the GPU together
     in_mix = {r.rid: r.E_elec for r in mixed.results}
     for req in reqs[:3]:

@@ -7,7 +7,7 @@ the CPU branches behind p.gpu=False, and be reversible.
 import types
 
 from pynof_gb300 import install as inst
-from pynof_gb300 import integrals, integrals_full, utils
+from pynof_gb300 import integrals, integrals_full, integrals_hf, utils
 
 
 def fake_pynof():
@@ -22,6 +22,8 @@ def fake_pynof():
     pynof.utils.computeLagrange2 = lambda *a: ("reference-cpu", "computeLagrange2")
     pynof.utils.ENERGY1r = lambda *a: ("reference-cpu", "ENERGY1r")
     pynof.utils.rotate_orbital = lambda *a: ("reference-cpu", "rotate_orbital")
+    pynof.integrals.computeD_HF = lambda *a: ("reference-cpu", "computeD_HF")
+    pynof.integrals.computeDalpha_HF = lambda *a: ("reference-cpu", "computeDalpha_HF")
     pynof.computeLagrange2 = pynof.utils.computeLagrange2
     pynof.ENERGY1r = pynof.utils.ENERGY1r
     pynof.rotate_orbital = pynof.utils.rotate_orbital
@@ -44,6 +46,8 @@ def test_install_rebinds_and_restores():
     p = types.SimpleNamespace(gpu=False)
     assert pynof.computeLagrange2(1, 2, 3, 4, 5, 6, 7, p) == ("reference-cpu", "computeLagrange2")
     assert pynof.utils.ENERGY1r(1, 2, 3, 4, 5, 6, 7, p) == ("reference-cpu", "ENERGY1r")
+    assert pynof.integrals.computeD_HF(1, p) == ("reference-cpu", "computeD_HF")
+    assert pynof.integrals.JK_HF_Full_GPU is integrals_hf.JK_HF_Full_GPU
     assert pynof.rotate_orbital(1, 2, p) == ("reference-cpu", "rotate_orbital")
     assert "p.gpu" in (pynof.rotate_orbital.__doc__ or "")  # the installed dispatcher
     # compute_integrals with p.gpu=False is the reference's

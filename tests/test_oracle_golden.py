@@ -101,3 +101,20 @@ def test_full_eri(name):
     p.RI = False
     elag, _ = orc.lagrange2(g["n_soft"], g["cj12"].copy(), g["ck12"].copy(), g["C"], g["H"], I, None, p)
     assert nrel(elag, g["elag2_full"]) < TOL
+
+
+@pytest.mark.parametrize("name", ["c1", "water"])
+def test_hf_jk_helpers(name):
+    """computeD_HF / computeDalpha_HF and their J, K (integrals.py:490-562);
+    the alpha goldens follow JKalpha_HF_Full_GPU (the einsum route)."""
+    g = load_golden(name)
+    p = param_for(name)
+    I = orc.eri_from_b(g["b"])
+    D = orc.density_hf(g["C"], 0, p.nbeta)
+    assert nrel(D, g["D_hf"]) < TOL
+    J, K = orc.jk_hf_full(D, I)
+    assert nrel(J, g["J_hf"]) < TOL and nrel(K, g["K_hf"]) < TOL
+    Da = orc.density_hf(g["C"], p.nbeta, p.nbeta + 2)
+    assert nrel(Da, g["Da_hf"]) < TOL
+    Ja, Ka = orc.jk_hf_full(Da, I)
+    assert nrel(Ja, g["Ja_hf"]) < TOL and nrel(Ka, g["Ka_hf"]) < TOL
