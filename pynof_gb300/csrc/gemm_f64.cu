@@ -179,6 +179,63 @@ __global__ void __launch_bounds__(THREADS) gemm_f64_kernel(const GemmF64 g) {
   }
 }
 
+// Small outputs: one warp per 8 x 8 block of C, DMMA m8n8k4 straight from
+// global memory (operands of small GEMMs sit in L2), loads batched UNR k-steps
+// ahead.  GB300's FP64 rate per SM is low (~7 GFLOP/s), so a GEMM that gives
+// the 64 x 64 kernel fewer CTAs than SMs is latency-bound on a few SMs; 8 x 8
+// blocks spread it over the whole GPU.
+template <int UNR>
+__global__ void __launch_bounds__(32) gemm_f64_small_kernel(const GemmF64 g) {
+  const int lane = threadIdx.x;
+  const int m0 = blockIdx.y * 8, n0 = blockIdx.x * 8;
+  const long long bz = blockIdx.z;
+  if (g.sym == SYM_ROWCOL && m0 > n0) return;
+  if (g.sym == SYM_PAIRCOL) {
+    const int j1 = min(n0 + 8, g.N) - 1;
+    const int ma = n0 / g.pair_n, mb = j1 / g.pair_n;
+    if (ma == mb && (j1 % g.pair_n) < ma) return;
+  }
+  const int gq = lane >> 2, tq = lane & 3;
+  const int ia = m0 + gq, jb = n0 + gq;  // A row / B column of this lane's fragments
+  const bool iok = ia < g.M, jok = jb < g.N;
+  const double* __restrict__ Ab = g.A.p + bz * g.A.sb + (iok ? g.A.r.at(ia) : 0);
+  const double* __restrict__ Bb = g.B.p + bz * g.B.sb + (jok ? g.B.c.at(jb) : 0);
+  double c0 = 0.0, c1 = 0.0;
+  for (int k0 = 0; k0 < g.K; k0 += 4 * UNR) {
+    double a[UNR], b[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int k = k0 + 4 * u + tq;
+      const bool kok = k < g.K;
+      a[u] = (iok && kok) ? __ldg(Ab + g.A.c.at(k)) : 0.0;
+      b[u] = (jok && kok) ? __ldg(Bb + g.B.r.at(k)) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) dmma(c0, c1, a[u], b[u]);
+  }
+  double* __restrict__ Cb = g.C.p + bz * g.C.sb;
+  const int i = m0 + gq;
+  if (i >= g.M) return;
+  const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
+  const long long ri = g.C.r.at(i);
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const int j = n0 + 2 * tq + e;
+    if (j >= g.N) continue;
+    if (g.sym == SYM_ROWCOL && m0 == n0 && j < i) continue;  // the diagonal block's mirror writes these
+    double v = g.alpha * (e ? c1 : c0);
+    double* dst = Cb + ri + g.C.c.at(j);
+    if (g.beta != 0.0) v += g.beta * *dst;
+    *dst = v;
+    if (g.sym == SYM_ROWCOL && (mirror_rc || j > i)) {
+      Cb[g.C.r.at(j) + g.C.c.at(i)] = v;
+    } else if (g.sym == SYM_PAIRCOL) {
+      const int mm = j / g.pair_n, nn = j % g.pair_n;
+      if (nn > mm) Cb[ri + g.C.c.at((long long)nn * g.pair_n + mm)] = v;
+    }
+  }
+}
+
 }  // namespace
 
 int gemm_f64(const GemmF64& g, cudaStream_t stream) {
@@ -193,6 +250,12 @@ int gemm_f64(const GemmF64& g, cudaStream_t stream) {
   const long long gx = (g.N + BN - 1) / BN;
   GB_REQUIRE(gy <= 65535 && g.batch <= 65535 && gx <= 2147483647LL, GB_ERR_BAD_SHAPE,
              "gemm_f64: grid too large (M=%d N=%d batch=%d)", g.M, g.N, g.batch);
+  if (gx * gy * g.batch < 152 && g.M <= 65535 * 8) {
+    // fewer 64 x 64 tiles than SMs: spread 8 x 8 blocks over the GPU instead
+    const dim3 sgrid((unsigned)((g.N + 7) / 8), (unsigned)((g.M + 7) / 8), (unsigned)g.batch);
+    GB_LAUNCH(g.tag, stream, gemm_f64_small_kernel<4><<<sgrid, 32, 0, stream>>>(g));
+    return GB_OK;
+  }
   dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)g.batch);
   if (g.a_kfast && g.b_kfast)
     GB_LAUNCH(g.tag, stream, gemm_f64_kernel<true, true><<<grid, THREADS, 0, stream>>>(g));

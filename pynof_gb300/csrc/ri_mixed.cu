@@ -318,7 +318,34 @@ namespace {
 struct Lag2MixedWs {
   SlicedDesc Aall, Tt, Sx, Sy;
   double *Tf, *bMO, *Y, *X, *d, *w, *cjm;
+  double* part;  // ns partial exchange products (ns > 1)
+  int ns, kc;    // K splits of the exchange GEMM and K per split
 };
+
+// K splits of the ck exchange GEMM (M = nbf, N = nbf5, K = nbf5 naux): with
+// few output tiles the long K would run on a few CTAs, so it is cut into
+// ranges of >= 768 that run as a batch; the partial products are summed in a
+// fixed order (deterministic).
+int exchange_splits(int N, int P, int Q) {
+  const long long tiles = (long long)((N + 127) / 128) * ((P + 127) / 128);
+  const long long K = (long long)P * Q;
+  if (tiles >= 76 || K < 2 * 768) return 1;
+  long long s = (152 + tiles - 1) / tiles;
+  s = s < K / 768 ? s : K / 768;
+  s = s < 64 ? s : 64;
+  while (s > 1 && K % s != 0) --s;  // equal ranges: every split reads only its own K
+  return (int)s;
+}
+
+// elag[a][b] = sum_s part[s][a][b], a < N, b < P (elag row stride N)
+__global__ void sum_splits_kernel(const double* __restrict__ part, int ns, int N, int P, double* __restrict__ elag) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)N * P) return;
+  const long long NP = (long long)N * P;
+  double v = 0.0;
+  for (int s = 0; s < ns; ++s) v += part[s * NP + idx];
+  elag[(idx / P) * N + idx % P] = v;
+}
 
 template <class Cv>
 void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
@@ -327,13 +354,16 @@ void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
   SlicedDesc Tt = take_sliced(c, P, Q, N, S);
   auto* bmo = c.template take<double>((size_t)N * P * Q);
   auto* Y = c.template take<double>((size_t)P * P * Q);
-  SlicedDesc Sx = take_sliced(c, 1, N, P * Q, S);
-  SlicedDesc Sy = take_sliced(c, 1, P, P * Q, S);
+  const int ns = exchange_splits(N, P, Q);
+  const int kc = (int)(((long long)P * Q + ns - 1) / ns);  // K per split
+  SlicedDesc Sx = take_sliced(c, ns, N, kc, S);
+  SlicedDesc Sy = take_sliced(c, ns, P, kc, S);
+  auto* part = ns > 1 ? c.template take<double>((size_t)ns * N * P) : nullptr;
   auto* X = c.template take<double>((size_t)N * P);
   auto* d = c.template take<double>((size_t)P * Q);
   auto* wv = c.template take<double>((size_t)P * Q);
   auto* cjm = c.template take<double>((size_t)P * P);
-  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm};
+  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, ns, kc};
 }
 }  // namespace
 
@@ -391,13 +421,21 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   GB_TRY(gemm_f64(gw, s));
   GB_TRY(launch_add_scaled_rows(w.w, w.d, n, P, Q, nbeta, nalpha, s));
   GB_TRY(launch_make_ck_weighted(w.bMO, ck12, w.Y, P, Q, s));
-  // elag[a][b] = -sum_(q,l) bMO[a][(q,l)] Y[b][(q,l)]
-  GB_TRY(slice_operand(SliceSrc{w.bMO, 0, lin((long long)P * Q), lin(1), true}, w.Sx, s));
-  GB_TRY(slice_operand(SliceSrc{w.Y, 0, lin((long long)P * Q), lin(1), true}, w.Sy, s));
+  // elag[a][b] = -sum_(q,l) bMO[a][(q,l)] Y[b][(q,l)], K cut into w.ns equal
+  // ranges (split s = batch s: element (row, k) at row * P Q + s kc + k)
+  GB_TRY(slice_operand(SliceSrc{w.bMO, w.kc, lin((long long)P * Q), lin(1), true}, w.Sx, s));
+  GB_TRY(slice_operand(SliceSrc{w.Y, w.kc, lin((long long)P * Q), lin(1), true}, w.Sy, s));
   OzGemm ge{};
-  ge.M = N; ge.N = P; ge.K = P * Q; ge.batch = 1; ge.S = S;
-  ge.C = elag; ge.c_sb = 0; ge.c_r = lin(N); ge.c_c = lin(1);
+  ge.M = N; ge.N = P; ge.K = w.kc; ge.batch = w.ns; ge.S = S;
   ge.sym = SYM_NONE; ge.negate = 1; ge.tag = "ozaki_tc:ck_exchange";
-  GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
+  if (w.ns > 1) {
+    ge.C = w.part; ge.c_sb = (long long)N * P; ge.c_r = lin(P); ge.c_c = lin(1);
+    GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
+    const long long np = (long long)N * P;
+    GB_LAUNCH("sum_splits", s, sum_splits_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(w.part, w.ns, N, P, elag));
+  } else {
+    ge.C = elag; ge.c_sb = 0; ge.c_r = lin(N); ge.c_c = lin(1);
+    GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
+  }
   return launch_lagrange2_finish(w.bMO, w.w, Hmat, n, elag, N, P, Q, s);
 }
