@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--nmol", type=int, default=64)
     ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rate", type=float, default=10.0)
+    ap.add_argument("--nbf-min", type=int, default=24)
     ap.add_argument("--nbf-max", type=int, default=150)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--tol", type=float, default=1e-5)
@@ -486,7 +487,7 @@ def run_serve(args):
     from pynof_gb300 import serve
 
     torch.cuda.set_device(0)
-    reqs = serve.poisson_stream(args.requests, args.rate, 24, args.nbf_max, seed=11)
+    reqs = serve.poisson_stream(args.requests, args.rate, args.nbf_min, args.nbf_max, seed=11)
     out = {}
     for prec in ("mixed", "fp64"):
         srv = serve.Server(hbm_budget=150e9, slots=args.slots, precision=prec, nslices=args.nslices,
@@ -499,7 +500,8 @@ def run_serve(args):
         out[prec].pop("energies")
     line = {"metric": "served NOF solves: p50/p99 latency and solves/s", "unit": "solves/s",
             "value": out["mixed"]["solves_per_s"], "data": "synthetic",
-            "config": {"requests": args.requests, "rate_per_s": args.rate, "nbf": f"log-uniform 24..{args.nbf_max}",
+            "config": {"requests": args.requests, "rate_per_s": args.rate,
+                       "nbf": f"log-uniform {args.nbf_min}..{args.nbf_max}",
                        "naux": "4 nbf", "tol": args.tol, "maxit": args.maxit, "slots": args.slots,
                        "hbm_budget_gb": 150, "fp64_switch_grad": 1e-2},
             "mixed": out["mixed"], "plain_fp64": out["fp64"],

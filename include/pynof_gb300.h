@@ -159,6 +159,15 @@ size_t gb_jk_hf_full_workspace_f64(int nbf);
 int gb_jk_hf_full_f64(const double* D, const double* I, int nbf, double* J, double* K, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* Post-NOF four-index transforms from the 4-index tensor:
+ *   out[p][q][r][t] = sum C[m][p0+p] C[n][q0+q] I[m][n][s][l] C[s][r0+r] C[l][t0+t],
+ *   out [np][nq][nr][nt].  Replaces iajb_Full_GPU (pynof/integrals.py:626-638;
+ *   i, j in [no1, nalpha), a, b in [nalpha, nbf)) and pqrt_Full_GPU (:657-660;
+ *   every range [0, nbf)). */
+size_t gb_mo4_full_workspace_f64(int nbf, int nq, int nr, int nt);
+int gb_mo4_full_f64(const double* C, const double* I, int nbf, int p0, int np, int q0, int nq, int r0, int nr,
+                    int t0, int nt, double* out, void* workspace, size_t workspace_bytes, void* stream);
+
 /* A6  computeLagrange2, full ERI, closed shell (pynof/utils.py:302-326).  The
  *     diagonals of cj12 / ck12 are ignored. */
 size_t gb_lagrange2_full_workspace_f64(int nbf, int nbf5);

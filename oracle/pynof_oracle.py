@@ -297,6 +297,13 @@ def jk_hf_full(D, I):
     return J, K
 
 
+def mo4_full(C, I, p, q, r, t):
+    """sum C[m,p] C[n,q] I[m,n,s,l] C[s,r] C[l,t] over orbital ranges
+    (``integrals.py:611-623`` iajb_Full_jit, ``:651-654`` pqrt_Full_jit)."""
+    Cp, Cq, Cr, Ct = (C[:, a:b] for a, b in (p, q, r, t))
+    return np.einsum("mp,nq,mnsl,sr,lt->pqrt", Cp, Cq, I, Cr, Ct, optimize=True)
+
+
 def eri_from_b(b):
     """(mn|sl) = sum_Q b[m, n, Q] b[s, l, Q] (the exact RI identity)."""
     N, _, Q = b.shape

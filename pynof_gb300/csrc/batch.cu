@@ -122,7 +122,7 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
     tilesJ += ozaki_tiles(pj[i].g);
     OzGemm k{};
     k.S = S; k.M = N; k.N = N; k.K = Q; k.batch = P; k.bn = 128; k.sym = SYM_ROWCOL;
-    k.C = K[i]; k.c_sb = (long long)N * N; k.c_r = lin(N); k.c_c = lin(1);
+    k.C = K[i]; k.c_sb = (long long)N * N; k.c_r = lin(1); k.c_c = lin(N);  // symmetric: stored transposed
     pk[i] = OzProblem{w.T, w.T, k};
     tilesK += ozaki_tiles(pk[i].g);
   }

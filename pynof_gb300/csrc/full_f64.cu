@@ -325,3 +325,72 @@ extern "C" int gb_jk_hf_full_f64(const double* D, const double* I, int nbf, doub
   GB_REQUIRE(D && I && J && K, GB_ERR_INVALID_ARG, "gb_jk_hf_full_f64: null pointer");
   return jk_full_core(D, I, nbf, 1, J, K, static_cast<cudaStream_t>(stream));
 }
+
+// ---------------------------------------------------------------------------
+// Post-NOF four-index MO transforms (compute_iajb / compute_pqrt,
+// integrals.py:601-662): out[p][q][r][t] = sum_{m n s l} C[m][p0+p] C[n][q0+q]
+// I[m][n][s][l] C[s][r0+r] C[l][t0+t], as four quarter transforms.
+// ---------------------------------------------------------------------------
+extern "C" size_t gb_mo4_full_workspace_f64(int nbf, int nq, int nr, int nt) {
+  Sizer z;
+  const size_t N = nbf;
+  const size_t x1 = N * N * N * nt, x3 = N * (size_t)nq * nr * nt;
+  z.add<double>(x1 > x3 ? x1 : x3);  // X1 [m][n][s][t], later X3 [m][q][r][t]
+  z.add<double>(N * N * nr * nt);    // X2 [m][n][r][t]
+  return z.used;
+}
+
+extern "C" int gb_mo4_full_f64(const double* C, const double* I, int nbf, int p0, int np, int q0, int nq, int r0,
+                               int nr, int t0, int nt, double* out, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+  clear_error();
+  const int N = nbf;
+  GB_TRY(check_full(N, 1));
+  auto range_ok = [N](int a, int n) { return a >= 0 && n >= 0 && a + n <= N; };
+  GB_REQUIRE(range_ok(p0, np) && range_ok(q0, nq) && range_ok(r0, nr) && range_ok(t0, nt), GB_ERR_BAD_SHAPE,
+             "gb_mo4_full_f64: orbital ranges outside [0, nbf)");
+  GB_REQUIRE((long long)N * N * N <= 2147483647LL && (long long)nq * nr * nt <= 2147483647LL &&
+                 (long long)N * N * nr * nt <= 2147483647LL,
+             GB_ERR_BAD_SHAPE, "gb_mo4_full_f64: sizes too large");
+  GB_REQUIRE(C && I && out, GB_ERR_INVALID_ARG, "gb_mo4_full_f64: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_mo4_full_workspace_f64(N, nq, nr, nt), GB_ERR_WORKSPACE,
+             "gb_mo4_full_f64: workspace too small");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (np == 0 || nq == 0 || nr == 0 || nt == 0) return GB_OK;
+  Carve cv(workspace, workspace_bytes);
+  const size_t x1 = (size_t)N * N * N * nt, x3 = (size_t)N * nq * nr * nt;
+  double* X1 = cv.take<double>(x1 > x3 ? x1 : x3);
+  double* X2 = cv.take<double>((size_t)N * N * nr * nt);
+  const long long NN = (long long)N * N, RT = (long long)nr * nt, QRT = (long long)nq * RT;
+  GemmF64 g{};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_NONE; g.batch = 1;
+  g.tag = "gemm_f64:quarter";
+  // X1[(m,n,s)][t] = sum_l I[(m,n,s)][l] C[l][t0+t]
+  g.M = (int)(NN * N); g.N = nt; g.K = N;
+  g.A = {I, 0, lin(N), lin(1)};
+  g.B = {C + t0, 0, lin(N), lin(1)};
+  g.C = {X1, 0, lin(nt), lin(1)};
+  g.a_kfast = true; g.b_kfast = false;
+  GB_TRY(gemm_f64(g, s));
+  // X2[(m,n)][r][t] = sum_s C[s][r0+r] X1[(m,n)][s][t]     columns j = ((m,n), t)
+  g.M = nr; g.N = (int)(NN * nt); g.K = N;
+  g.A = {C + r0, 0, lin(1), lin(N)};
+  g.B = {X1, 0, lin(nt), split(nt, (long long)N * nt, 1)};
+  g.C = {X2, 0, lin(nt), split(nt, RT, 1)};
+  g.a_kfast = false; g.b_kfast = false;
+  GB_TRY(gemm_f64(g, s));
+  // X3[m][q][(r,t)] = sum_n C[n][q0+q] X2[m][n][(r,t)]     columns j = (m, (r,t)); over X1
+  double* X3 = X1;
+  g.M = nq; g.N = (int)(N * RT); g.K = N;
+  g.A = {C + q0, 0, lin(1), lin(N)};
+  g.B = {X2, 0, lin(RT), split(RT, N * RT, 1)};
+  g.C = {X3, 0, lin(RT), split(RT, QRT, 1)};
+  GB_TRY(gemm_f64(g, s));
+  // out[p][(q,r,t)] = sum_m C[m][p0+p] X3[m][(q,r,t)]
+  g.M = np; g.N = (int)QRT; g.K = N;
+  g.A = {C + p0, 0, lin(1), lin(N)};
+  g.B = {X3, 0, lin(QRT), lin(1)};
+  g.C = {out, 0, lin(QRT), lin(1)};
+  return gemm_f64(g, s);
+}
+

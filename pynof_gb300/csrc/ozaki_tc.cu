@@ -716,6 +716,319 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   }
 }
 
+// Persistent form (bf16 digits; outputs whose tile rows are the unit stride,
+// so the epilogue stores straight from registers and never parks results in
+// the stage buffers).  One CTA per SM walks the tiles t = blockIdx.x,
+// + gridDim.x, ...  The producer runs ahead across tile boundaries (the next
+// tile's first stages load during this tile's epilogue), and the epilogue
+// releases TMEM as soon as the last chunk is folded into registers, so the
+// next tile's MMAs overlap the conversion and stores.  Pipeline phases
+// (stages, chunks) count on across tiles.
+template <int S, int BN>
+__device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsigned char* smem_raw) {
+  using T = TileCfg<BN, 0>;
+  const OzGemm& g = a.g;
+  constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
+  constexpr bool has_inexact = (S + 1) > 4;
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t a_bytes = (uint32_t)S * TILE_BYTES, b_bytes = (uint32_t)S * T::B_TILE;
+  constexpr uint32_t stage_bytes = a_bytes + b_bytes;
+  constexpr uint32_t zs_bytes = BM * (BN + 1) * 8;  // same layout as cta_tile (smem_bytes)
+  constexpr uint32_t data_bytes = STAGES * stage_bytes > zs_bytes ? STAGES * stage_bytes : zs_bytes;
+  long long* e_roff = reinterpret_cast<long long*>(smem + data_bytes);
+  long long* e_mr = e_roff + BM;
+  long long* e_coff = e_mr + BM;
+  long long* e_mc = e_coff + BN;
+  int* e_srow = reinterpret_cast<int*>(e_mc + BN);
+  int* e_scol = e_srow + BM;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + data_bytes + epi_table_bytes(BN));
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
+  const uint32_t sbase = smem_u32(smem);
+  const uint32_t bar0 = smem_u32(bars);
+  auto full_bar = [&](int st) { return bar0 + 8u * st; };
+  auto empty_bar = [&](int st) { return bar0 + 8u * (STAGES + st); };
+  const uint32_t accfull_bar = bar0 + 8u * (2 * STAGES), accempty_bar = bar0 + 8u * (2 * STAGES + 1),
+                 done_bar = bar0 + 8u * (2 * STAGES + 2);
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(full_bar(i), 1);
+      mbar_init(empty_bar(i), 1);
+    }
+    mbar_init(accfull_bar, 1);
+    mbar_init(accempty_bar, NUM_EPI_WARPS);
+    mbar_init(done_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(const_cast<uint32_t*>(tmem_slot))),
+                 "r"(T::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int nkb = (g.K + BK - 1) / BK;
+  const int nchunks = (nkb + CH - 1) / CH;
+  const int tstep = gridDim.x;
+
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      int gkb = 0;  // stages issued so far (all tiles)
+      bool aborted = false;
+      for (int t = blockIdx.x; t < ntiles && !aborted; t += tstep) {
+        int bz, m0, n0;
+        if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
+        const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
+        const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
+                                  (long long)(m0 / BM) * a.A.kblocks() * a_bytes;
+        const int rb = n0 / SL_ROWS, r0 = n0 % SL_ROWS;
+        const unsigned char* gbp = reinterpret_cast<const unsigned char*>(a.B.planes) + bbz * a.B.batch_bytes() +
+                                   (long long)rb * a.B.kblocks() * (S * TILE_BYTES) + (r0 / 8) * 128;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int st = gkb % STAGES;
+          const uint32_t ph = (uint32_t)((gkb / STAGES) & 1);
+          if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag)) {
+            signal_abort(abort_flag);
+            aborted = true;
+            break;
+          }
+          mbar_expect_tx(full_bar(st), stage_bytes);
+          const uint32_t sa = sbase + st * stage_bytes;
+          bulk_load(sa, ga + (long long)kb * a_bytes, a_bytes, full_bar(st));
+          const unsigned char* gblk = gbp + (long long)kb * (S * TILE_BYTES);
+          if (BN == SL_ROWS) {
+            bulk_load(sa + a_bytes, gblk, b_bytes, full_bar(st));
+          } else {
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2)
+#pragma unroll
+              for (int kg = 0; kg < 2; ++kg)
+                bulk_load(sa + a_bytes + s2 * T::B_TILE + kg * (BN * 16), gblk + s2 * TILE_BYTES + kg * 2048, BN * 16,
+                          full_bar(st));
+          }
+          ++gkb;
+        }
+      }
+      if (*abort_flag) {
+        for (int k = gkb > STAGES ? gkb - STAGES : 0; k < gkb; ++k)
+          mbar_wait(full_bar(k % STAGES), (uint32_t)((k / STAGES) & 1), nullptr);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int gkb = 0, gch = 0;
+      bool aborted = false;
+      for (int t = blockIdx.x; t < ntiles && !aborted; t += tstep) {
+        int bz, m0, n0;
+        if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
+        const int n_valid = min(BN, g.N - n0);
+        const int n_mma = (n_valid + 15) & ~15;
+        const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
+        bool f_started = false;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int st = gkb % STAGES;
+          if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag)) {
+            signal_abort(abort_flag);
+            aborted = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = sbase + st * stage_bytes;
+          const uint64_t da = desc_tile(sa, BM), db = desc_tile(sa + a_bytes, BN);
+          const int c = kb / CH;
+          const bool first = (kb % CH) == 0;
+          // a new tile (or, with fdrain, every chunk) must wait until the
+          // epilogue has taken everything out of TMEM; inside a tile the FP32
+          // group may run ahead while the exact groups drain
+          if (first && gch > 0 && (c == 0 || g.fdrain)) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag)) {
+              signal_abort(abort_flag);
+              aborted = true;
+              break;
+            }
+            tc_fence_after();
+          }
+          if (g.fdrain && first) f_started = false;
+          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
+          if (!g.fdrain && first && c > 0) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag)) {
+              signal_abort(abort_flag);
+              aborted = true;
+              break;
+            }
+            tc_fence_after();
+          }
+          issue_exact<S, BN>(tmem, da, db, idesc, first);
+          if ((kb % CH) == CH - 1 || kb == nkb - 1) {
+            mma_commit(accfull_bar);
+            ++gch;
+          }
+          mma_commit(empty_bar(st));
+          ++gkb;
+        }
+      }
+      mma_commit(done_bar);
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    constexpr int CW = T::CW;
+    const int q = warp & 3;
+    const int cg = (warp - 2) >> 2;
+    const int et = threadIdx.x - 64;
+    const uint32_t lbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * CW);
+    const float two_frac = __int_as_float((127 + a.frac) << 23);
+    const float upE = __int_as_float((127 + 7 * gE) << 23);
+    const int row = q * 32 + lane;
+    int gch = 0;
+    for (int t = blockIdx.x; t < ntiles; t += tstep) {
+      int bz, m0, n0;
+      if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
+      // every epilogue warp is done with the previous tile's tables
+      if (epi_barrier_any(*abort_flag != 0)) break;
+      {
+        const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
+        if (et < BM) {
+          const int i = m0 + et;
+          const bool in = i < g.M;
+          long long mr = -1;
+          if (in && g.sym == SYM_ROWCOL) mr = g.c_c.at(i);
+          if (in && g.sym == SYM_PAIRROW) {
+            const int mm = i / g.pair_n, nn = i % g.pair_n;
+            if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
+          }
+          e_roff[et] = in ? g.c_r.at(i) : 0;
+          e_mr[et] = mr;
+          e_srow[et] = in ? a.A.exps[abz * g.M + i] : 0;
+        } else if (et < BM + BN) {
+          const int c = et - BM, jj = n0 + c;
+          const bool in = jj < g.N;
+          long long mc = -1;
+          if (in && g.sym == SYM_ROWCOL) mc = g.c_r.at(jj);
+          if (in && g.sym == SYM_PAIRCOL) {
+            const int mm = jj / g.pair_n, nn = jj % g.pair_n;
+            if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
+          }
+          e_coff[c] = in ? g.c_c.at(jj) : 0;
+          e_mc[c] = mc;
+          e_scol[c] = in ? a.B.exps[bbz * g.N + jj] - 7 * gE - a.frac : 0;
+        }
+      }
+      epi_barrier_any(false);  // tables visible
+      const int n_valid = min(BN, g.N - n0);
+      const bool cols_live = cg * CW < n_valid;  // warp-uniform
+      long long R[CW];
+#pragma unroll
+      for (int j = 0; j < CW; ++j) R[j] = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunks; ++c) {
+        const bool got = mbar_wait(accfull_bar, (uint32_t)(gch & 1), abort_flag);
+        if (!__all_sync(0xffffffffu, got)) {
+          signal_abort(abort_flag);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const int fr = g.fdrain ? a.frac : 0;
+#pragma unroll
+        for (int h = 0; h < (cols_live ? CW / 4 : 0); ++h) {
+          uint32_t v2[4], v3[4], v4[4];
+          tmem_ld4_async(lbase + (uint32_t)(h * 4), v2);
+          if (gE >= 3) tmem_ld4_async(lbase + (uint32_t)(BN + h * 4), v3);
+          if (gE >= 4) tmem_ld4_async(lbase + (uint32_t)(2 * BN + h * 4), v4);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int i2 = magic_int(__uint_as_float(v2[j]), 16384.0f);
+            long long acc;
+            if (gE == 2) {
+              acc = i2;
+            } else if (gE == 3) {
+              acc = (long long)i2 * 128 + magic_int(__uint_as_float(v3[j]), 2097152.0f);
+            } else {
+              const int i34 = magic_int(__uint_as_float(v3[j]), 2097152.0f) * 128 +
+                              magic_int(__uint_as_float(v4[j]), 268435456.0f);
+              acc = (long long)i2 * 16384 + i34;
+            }
+            R[h * 4 + j] += (long long)((unsigned long long)acc << fr);
+          }
+        }
+        const bool last = c == nchunks - 1;
+        if (has_inexact && cols_live && (g.fdrain || last)) {
+          // the FP32 group: drained every chunk (fdrain) or folded in at the end
+#pragma unroll
+          for (int h = 0; h < CW / 8; ++h) {
+            uint32_t v[8];
+            tmem_ld8_async(lbase + (uint32_t)(3 * BN + h * 8), v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const long long f = split_round(__uint_as_float(v[j]) * upE, a.frac, two_frac);
+              R[h * 8 + j] = g.fdrain ? R[h * 8 + j] + f : (long long)((unsigned long long)R[h * 8 + j] << a.frac) + f;
+            }
+          }
+        } else if (last && !g.fdrain) {
+#pragma unroll
+          for (int j = 0; j < CW; ++j) R[j] = (long long)((unsigned long long)R[j] << a.frac);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(accempty_bar);  // TMEM free for the next chunk / tile
+        ++gch;
+      }
+      if (!ok) continue;  // the next tile's barrier sees the abort flag in every warp
+      // convert and store from registers (rows are the output's unit stride)
+      double* Cb = g.C + (long long)bz * g.c_sb;
+      const bool mirror_rc = (g.sym == SYM_ROWCOL) && (m0 != n0);
+      const int rlim = min(BM, g.M - m0), clim = min(BN, g.N - n0);
+      if (row < rlim) {
+        const int srow = e_srow[row];
+        const long long ro = e_roff[row], mr = e_mr[row];
+#pragma unroll
+        for (int j = 0; j < CW; ++j) {
+          const int c = cg * CW + j;
+          if (c >= clim) continue;
+          const double val = scaled_to_double(R[j], srow + e_scol[c], g.negate);
+          const long long co = e_coff[c];
+          Cb[ro + co] = val;
+          if (mirror_rc) {
+            Cb[e_mc[c] + mr] = val;
+          } else if (g.sym == SYM_PAIRCOL) {
+            const long long mc = e_mc[c];
+            if (mc >= 0) Cb[ro + mc] = val;
+          } else if (g.sym == SYM_PAIRROW) {
+            if (mr >= 0) Cb[mr + co] = val;
+          }
+        }
+      }
+    }
+  }
+
+  __syncthreads();
+  if (warp == 1) {
+    if (*abort_flag) mbar_wait(done_bar, 0, nullptr);
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::TMEM_COLS) : "memory");
+  }
+}
+
+template <int S, int BN>
+__global__ void __maxnreg__(MAX_REGS) ozaki_persistent_kernel(const __grid_constant__ KArgs a, int ntiles) {
+  extern __shared__ unsigned char smem_raw[];
+  if (*(volatile int*)&g_tc_status != 0) return;
+  cta_persistent<S, BN>(a, ntiles, smem_raw);
+}
+
 template <int S, int BN, int KIND>
 __global__ void __maxnreg__(MAX_REGS) ozaki_kernel(const __grid_constant__ KArgs a) {
   extern __shared__ unsigned char smem_raw[];
@@ -785,6 +1098,18 @@ GroupedFn grouped_for(int S) {
   }
 }
 
+using PersistFn = void (*)(KArgs, int);
+PersistFn persistent_for(int S) {
+  switch (S) {
+    case 1: return ozaki_persistent_kernel<1, 128>;
+    case 2: return ozaki_persistent_kernel<2, 128>;
+    case 3: return ozaki_persistent_kernel<3, 128>;
+    case 4: return ozaki_persistent_kernel<4, 128>;
+    case 5: return ozaki_persistent_kernel<5, 128>;
+    default: return ozaki_persistent_kernel<6, 128>;
+  }
+}
+
 KernelFn kernel_for(int S, int BN) {
   return BN == 32 ? single_for<32>(S) : BN == 64 ? single_for<64>(S) : single_for<128>(S);
 }
@@ -793,6 +1118,8 @@ GroupedFn grouped_kernel_for(int S, int BN) {
 }
 
 // Opt every instantiation in to its dynamic shared memory once per device.
+int g_num_sms[64] = {0};
+
 int configure_device() {
   static std::mutex mu;
   static int configured[64] = {0};
@@ -809,6 +1136,12 @@ int configure_device() {
           cudaFuncSetAttribute(grouped_kernel_for(sl, bn), cudaFuncAttributeMaxDynamicSharedMemorySize, sm),
           "cudaFuncSetAttribute"));
     }
+  for (int sl = 1; sl <= 6; ++sl)
+    GB_TRY(cuda_status(cudaFuncSetAttribute(persistent_for(sl), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem_bytes(sl, 128)),
+                       "cudaFuncSetAttribute"));
+  GB_TRY(cuda_status(cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev),
+                     "cudaDeviceGetAttribute"));
   configured[dev] = 1;
   return GB_OK;
 }
@@ -881,8 +1214,18 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   GB_TRY(configure_device());
   const KArgs ka = make_args(A, B, g);
   const long long tiles = ozaki_tiles(g);
+  // outputs whose tile rows are the unit stride take the persistent kernel
+  const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int nsm = (dev >= 0 && dev < 64 && g_num_sms[dev] > 0) ? g_num_sms[dev] : 0;
   const int pi = prof_begin(g.tag, stream);
-  kernel_for(g.S, g.bn)<<<grid_for(tiles), THREADS, smem_bytes(g.S, g.bn), stream>>>(ka);
+  if (g.S >= 1 && g.S <= 6 && g.bn == 128 && rows_fast && nsm > 0 && tiles < (1LL << 30)) {
+    const long long grid = tiles < nsm ? tiles : nsm;
+    persistent_for(g.S)<<<(unsigned)grid, THREADS, smem_bytes(g.S, 128), stream>>>(ka, (int)tiles);
+  } else {
+    kernel_for(g.S, g.bn)<<<grid_for(tiles), THREADS, smem_bytes(g.S, g.bn), stream>>>(ka);
+  }
   prof_end(pi, stream);
   const cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return launch_error(g.tag, le, g.S, g.bn);

@@ -153,7 +153,9 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s));
   OzGemm gk{};
   gk.M = N; gk.N = N; gk.K = Q; gk.batch = P; gk.S = S;
-  gk.C = K; gk.c_sb = (long long)N * N; gk.c_r = lin(N); gk.c_c = lin(1);
+  // K_q is symmetric: the tile is stored transposed (rows on the unit stride),
+  // which lets the epilogue store straight from its TMEM-lane layout
+  gk.C = K; gk.c_sb = (long long)N * N; gk.c_r = lin(1); gk.c_c = lin(N);
   gk.sym = SYM_ROWCOL; gk.tag = "ozaki_tc:K";
   GB_TRY(ozaki_gemm(w.T, w.T, gk, s));
   return GB_OK;

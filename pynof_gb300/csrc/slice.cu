@@ -95,10 +95,22 @@ __global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, Slice
   const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
   const int e = rok ? dst.exps[b * dst.rows + r] : 0;
   double xs[8];
+  const double* p8 = base + k0;
+  if (rok && src.kfast && src.k.div == 0 && src.k.s0 == 1 && k0 + 8 <= dst.K &&
+      (reinterpret_cast<uintptr_t>(p8) & 15) == 0) {
+    // contiguous, 16-byte aligned k run: four 16-byte loads
 #pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    const int k = k0 + u;
-    xs[u] = (rok && k < dst.K) ? base[src.k.at(k)] : 0.0;
+    for (int u = 0; u < 4; ++u) {
+      const double2 v = __ldg(reinterpret_cast<const double2*>(p8) + u);
+      xs[2 * u] = v.x;
+      xs[2 * u + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = k0 + u;
+      xs[u] = (rok && k < dst.K) ? base[src.k.at(k)] : 0.0;
+    }
   }
 #pragma unroll
   for (int u = 0; u < 8; ++u) make_digits<S>(xs[u], e, dg[u]);

@@ -23,6 +23,8 @@ GPU_FUNCTIONS = {
     "utils.computeF_RC_GPU": utils.computeF_RC_GPU,
     "integrals.JK_HF_Full_GPU": integrals_hf.JK_HF_Full_GPU,
     "integrals.JKalpha_HF_Full_GPU": integrals_hf.JKalpha_HF_Full_GPU,
+    "integrals.iajb_Full_GPU": integrals_full.iajb_Full_GPU,
+    "integrals.pqrt_Full_GPU": integrals_full.pqrt_Full_GPU,
 }
 
 

@@ -24,3 +24,27 @@ def Integrals_MO_Full_GPU(C, H, I, p):
     """H_mat (nbf, nbf5), I_MO (nbf, nbf5, nbf5, nbf5) on the device --
     ``pynof/integrals.py:693-698``."""
     return ops.mo_full(as_device(C), as_device(H), as_device(I), p.nbf5)
+
+
+def iajb_Full_GPU(C, I, p):
+    """``pynof/integrals.py:626-638``: (ia|jb) over occupied i, j in
+    [no1, nalpha) and virtual a, b in [nalpha, nbf); host numpy out."""
+    occ, vir = (p.no1, p.nalpha), (p.nalpha, p.nbf)
+    return to_host(ops.mo4_full(as_device(C), as_device(I), occ, vir, occ, vir))
+
+
+def compute_iajb(C, I, b_mnl, p):
+    """``pynof/integrals.py:601-608`` (the GPU branch)."""
+    return iajb_Full_GPU(C, I, p)
+
+
+def pqrt_Full_GPU(C, I, p):
+    """``pynof/integrals.py:657-660``: the full four-index MO transform."""
+    a = (0, p.nbf)
+    return to_host(ops.mo4_full(as_device(C), as_device(I), a, a, a, a))
+
+
+def compute_pqrt(C, I, b_mnl, p):
+    """``pynof/integrals.py:641-648`` (the GPU branch)."""
+    return pqrt_Full_GPU(C, I, p)
+

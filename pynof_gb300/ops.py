@@ -287,6 +287,20 @@ def ri_factor(mnk: torch.Tensor, M: torch.Tensor, nslices: int | None = None) ->
     return b
 
 
+def mo4_full(C: torch.Tensor, I: torch.Tensor, p, q, r, t) -> torch.Tensor:
+    """out[p][q][r][t] = sum C[m,p] C[n,q] I[m,n,s,l] C[s,r] C[l,t] over the
+    orbital ranges p, q, r, t (each a (start, stop) pair)."""
+    N = C.shape[0]
+    _require(C, (N, N), "C")
+    _require(I, (N, N, N, N), "I")
+    (p0, p1), (q0, q1), (r0, r1), (t0, t1) = p, q, r, t
+    out = torch.empty((p1 - p0, q1 - q0, r1 - r0, t1 - t0), dtype=_F64, device=C.device)
+    wp, wn = _ws("gb_mo4_full_workspace_f64", N, q1 - q0, r1 - r0, t1 - t0, device=C.device)
+    _lib.call("gb_mo4_full_f64", _ptr(C), _ptr(I), N, p0, p1 - p0, q0, q1 - q0, r0, r1 - r0, t0, t1 - t0,
+              _ptr(out), wp, wn, _stream(C.device))
+    return out
+
+
 def density_hf(C: torch.Tensor, j0: int, j1: int) -> torch.Tensor:
     """D = sum_{j0 <= j < j1} C[:, j] C[:, j]^T (computeD_HF / computeDalpha_HF)."""
     N = C.shape[0]

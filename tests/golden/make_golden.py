@@ -233,6 +233,8 @@ def run_case(pynof, name, workload, seed, full, jit):
         checks["JKalpha_HF_jit_D_J_diagonal_max"] = float(max(np.abs(np.diag(Dj)).max(), np.abs(np.diag(Jj)).max()))
         checks["JKalpha_HF_jit_J_vs_gpu_route"] = nrel(Jj, Ja_hf)  # differs: D's diagonal is missing
         out.update(D_hf=D_hf, J_hf=J_hf, K_hf=K_hf, Da_hf=Da_hf, Ja_hf=Ja_hf, Ka_hf=Ka_hf)
+        # post-NOF four-index transforms (integrals.py:601-662)
+        out.update(iajb=pynof.compute_iajb(C, I, [], pf), pqrt=pynof.compute_pqrt(C, I, [], pf))
 
     meta = dict(case=name, workload=workload, seed=seed, sizes=synthetic.WORKLOADS[workload],
                 numpy=np.__version__, checks=checks)

@@ -128,3 +128,15 @@ def test_hf_jk_golden(torch_cuda, name):
     assert nrel(Ja, g["Ja_hf"]) < 1e-10 and nrel(Ka, g["Ka_hf"]) < 1e-10
     assert nrel(integrals_hf.computeDalpha_HF(g["C"], pa), g["Da_hf"]) < 1e-12
 
+
+@pytest.mark.parametrize("name", ["c1", "water"])
+def test_post_nof_transforms_golden(torch_cuda, name):
+    """compute_iajb / compute_pqrt drop-ins against the reference's outputs."""
+    from pynof_gb300 import integrals, integrals_full
+
+    g = load_golden(name)
+    p = param_for(GOLDEN_CASES[name])
+    I = integrals.upload_integrals(np.einsum("mnQ,slQ->mnsl", g["b"], g["b"]), None)[0]
+    assert nrel(integrals_full.compute_iajb(g["C"], I, None, p), g["iajb"]) < 1e-10
+    assert nrel(integrals_full.compute_pqrt(g["C"], I, None, p), g["pqrt"]) < 1e-10
+

@@ -118,3 +118,14 @@ def test_hf_jk_helpers(name):
     assert nrel(Da, g["Da_hf"]) < TOL
     Ja, Ka = orc.jk_hf_full(Da, I)
     assert nrel(Ja, g["Ja_hf"]) < TOL and nrel(Ka, g["Ka_hf"]) < TOL
+
+
+@pytest.mark.parametrize("name", ["c1", "water"])
+def test_post_nof_transforms(name):
+    """compute_iajb / compute_pqrt (integrals.py:601-662)."""
+    g = load_golden(name)
+    p = param_for(name)
+    I = orc.eri_from_b(g["b"])
+    occ, vir, full = (p.no1, p.nalpha), (p.nalpha, p.nbf), (0, p.nbf)
+    assert nrel(orc.mo4_full(g["C"], I, occ, vir, occ, vir), g["iajb"]) < TOL
+    assert nrel(orc.mo4_full(g["C"], I, full, full, full, full), g["pqrt"]) < TOL
