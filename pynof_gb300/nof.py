@@ -35,33 +35,51 @@ def _pairs(p):
     return out
 
 
+@functools.lru_cache(maxsize=64)
+def _pair_index(no1, ndoc, ndns, ncwo):
+    i = np.arange(ndoc)
+    s = no1 + i
+    weak = (no1 + ndns + (ndoc - i - 1))[:, None] + ndoc * np.arange(ncwo)[None, :]
+    gam = (ndoc - i - 1)[:, None] + ndoc * np.arange(ncwo)[None, :]
+    block = np.concatenate([s[:, None], weak], axis=1)  # (ndoc, 1 + ncwo): strong first
+    return s, weak, gam, block
+
+
 def ocupacion_softmax(gamma, p):
     """Occupations n (nbf5,) and dn/dgamma (nbf5, nv) from the softmax
     parameterisation (``pnof.py:770-809``): each strong orbital and its weak
-    partners share one softmax with a zero logit for the strong orbital."""
+    partners share one softmax with a zero logit for the strong orbital.
+    All pairs at once (their index sets are disjoint)."""
     n = np.zeros(p.nbf5)
     dn = np.zeros((p.nbf5, p.nv))
     n[p.no1 + p.ndoc: p.no1 + p.ndns] = 1.0 if p.HighSpin else 0.5
-    for i, (_, weak, gam) in enumerate(_pairs(p)):
-        x = gamma[gam]
-        top = x.max() if len(x) else 0.0
-        if top < 700.0:
-            e = np.exp(x)
-            den = 1.0 + e.sum()
-            ns = 1.0 / den
-            nw = e / den
-        else:
-            # logits a line search pushed past exp's range: the same softmax,
-            # shifted by its largest logit
-            e = np.exp(x - top)
-            den = np.exp(-top) + e.sum()
-            ns = np.exp(-top) / den
-            nw = e / den
-        # the reference writes the strong occupation at index i (pnof.py:793)
-        n[i] = ns
-        n[weak] = nw
-        dn[i, gam] = -ns * nw
-        dn[np.ix_(weak, gam)] = np.diag(nw) - np.outer(nw, nw)
+    if p.ndoc == 0:
+        return n, dn
+    _, weak, gam, _ = _pair_index(p.no1, p.ndoc, p.ndns, p.ncwo)
+    x = np.asarray(gamma)[gam]  # (ndoc, ncwo)
+    top = x.max(axis=1) if p.ncwo else np.zeros(p.ndoc)
+    e = np.exp(np.minimum(x, 700.0))
+    den = 1.0 + e.sum(axis=1)
+    ns = 1.0 / den
+    nw = e / den[:, None]
+    big = top >= 700.0
+    if np.any(big):
+        # logits a line search pushed past exp's range: the same softmax,
+        # shifted by its largest logit
+        xb, tb = x[big], top[big]
+        eb = np.exp(xb - tb[:, None])
+        denb = np.exp(-tb) + eb.sum(axis=1)
+        ns[big] = np.exp(-tb) / denb
+        nw[big] = eb / denb[:, None]
+    rows = np.arange(p.ndoc)
+    # the reference writes the strong occupation at index i (pnof.py:793)
+    n[rows] = ns
+    n[weak] = nw
+    dn[rows[:, None], gam] = -ns[:, None] * nw
+    blk = -nw[:, :, None] * nw[:, None, :]
+    ar = np.arange(p.ncwo)
+    blk[:, ar, ar] += nw
+    dn[weak[:, :, None], gam[:, None, :]] = blk
     return n, dn
 
 
@@ -69,10 +87,11 @@ def cjckd8(n, p):
     """GNOF coefficients C^J, C^K (nbf5, nbf5) (``pnof.py:350-422``)."""
     no1, nb, na = p.no1, p.nbeta, p.nalpha
     nd = np.zeros_like(n)
-    for s, weak, _ in _pairs(p):
+    if p.ndoc:
+        s, weak, _, _ = _pair_index(p.no1, p.ndoc, p.ndns, p.ncwo)
         F = np.exp(-((1.0 - n[s]) / H_CUT) ** 2)
         nd[s] = n[s] * F
-        nd[weak] = n[weak] * F
+        nd[weak] = n[weak] * F[:, None]
     nd12 = np.sqrt(nd)
     fi = np.sqrt(np.clip(n * (1.0 - n), 0.0, None))
     cj = 2.0 * np.outer(n, n)
@@ -93,13 +112,16 @@ def cjckd8(n, p):
     ck[S, W] += np.outer(nd12[S], nd12[W]) - np.outer(nd[S], nd[W])
     ck[W, S] += np.outer(nd12[W], nd12[S]) - np.outer(nd[W], nd[S])
     ck[W, W] += -np.outer(nd12[W], nd12[W]) - np.outer(nd[W], nd[W])
-    for s, weak, _ in _pairs(p):
-        cj[s, weak] = 0.0
-        cj[weak, s] = 0.0
-        cj[np.ix_(weak, weak)] = 0.0
-        ck[s, weak] = np.sqrt(n[s] * n[weak])
-        ck[weak, s] = np.sqrt(n[s] * n[weak])
-        ck[np.ix_(weak, weak)] = -np.sqrt(np.outer(n[weak], n[weak]))
+    if p.ndoc:
+        s, weak, _, _ = _pair_index(p.no1, p.ndoc, p.ndns, p.ncwo)
+        sc = s[:, None]
+        cj[sc, weak] = 0.0
+        cj[weak, sc] = 0.0
+        cj[weak[:, :, None], weak[:, None, :]] = 0.0
+        sw = np.sqrt(n[s][:, None] * n[weak])
+        ck[sc, weak] = sw
+        ck[weak, sc] = sw
+        ck[weak[:, :, None], weak[:, None, :]] = -np.sqrt(n[weak][:, :, None] * n[weak][:, None, :])
     return cj, ck
 
 
@@ -162,6 +184,102 @@ def calce(n, cj12, ck12, J_MO, K_MO, H_core, p):
     dj = np.diagonal(J_MO)
     E = 2.0 * np.dot(n, H_core) + np.dot(n[: p.nbeta], dj[: p.nbeta]) + np.dot(n[p.nalpha: P], dj[p.nalpha: P])
     return E + np.sum(cj12 * J_MO.T) - np.sum(ck12 * K_MO.T)
+
+
+# ---------------------------------------------------------------------------
+# Occupation gradient by contraction.  calcoccg above materialises
+# dC^J/dgamma and dC^K/dgamma as (nbf5, nbf5, nv) tensors and contracts them
+# with J_MO, K_MO; scipy's CG calls it thousands of times per occoptr, so the
+# O(nbf5^2 nv) tensors dominate a served solve.  Every term of der_cjckd8 is an
+# outer product u[a, k] v[b] on a block of (a, b), so its contraction with a
+# matrix Y is u[A]^T (Y[A, B] v[B]): O(nbf5^2 + nbf5 nv).  The intra-pair
+# blocks, which der_cjckd8 overwrites, are corrected pair by pair on small
+# (1 + ncwo)^2 blocks.  Closed shell without singly occupied orbitals (the
+# served and benchmarked case); other structures use calcoccg.
+# ---------------------------------------------------------------------------
+def _fast_ok(p):
+    return p.MSpin == 0 and p.nsoc == 0 and p.ncwo >= 1 and p.ndoc >= 1
+
+
+def calcoccg_fast(gamma, J_MO, K_MO, H_core, p):
+    """dE/dgamma equal to :func:`calcoccg` (same terms, contracted without
+    the (nbf5, nbf5, nv) derivative tensors)."""
+    if not _fast_ok(p):
+        return calcoccg(gamma, J_MO, K_MO, H_core, p)
+    P, no1, nb, na = p.nbf5, p.no1, p.nbeta, p.nalpha
+    n, dn = ocupacion_softmax(gamma, p)
+    s_idx, weak, gam, block = _pair_index(p.no1, p.ndoc, p.ndns, p.ncwo)
+    # occupation-derived vectors of der_cjckd8
+    ns = n[s_idx]
+    coc = (1.0 - ns) / H_CUT
+    F = np.exp(-coc ** 2)
+    dF = 2.0 * coc / H_CUT
+    nd = np.zeros(P)
+    dnd = np.zeros_like(dn)
+    nd[s_idx] = ns * F
+    nd[weak] = n[weak] * F[:, None]
+    dnd[s_idx] = F[:, None] * dn[s_idx] * (1.0 + ns * dF)[:, None]
+    dnd[weak] = F[:, None, None] * (dn[weak] + dF[:, None, None] * n[weak][:, :, None] * dn[s_idx][:, None, :])
+    nd12 = np.sqrt(nd)
+    dnd12 = 0.5 * dnd / np.maximum(nd12, 1e-15)[:, None]
+    fi = np.sqrt(np.clip(n * (1.0 - n), 0.0, None))
+    dfi = np.zeros_like(dn)
+    dfi[no1:] = ((1.0 - 2.0 * n[no1:]) / (2.0 * np.maximum(fi[no1:], 1e-15)))[:, None] * dn[no1:]
+    YJ, YK = J_MO.T, K_MO.T  # sum_ij D[i, j, k] X[j, i] = sum_ij D[i, j, k] Y[i, j]
+    S, W = slice(no1, nb), slice(na, P)
+
+    def blk(u, v, A, B, Y):  # sum_{a in A, b in B} u[a, k] v[b] Y[a, b]
+        return u[A].T @ (Y[A, B] @ v[B])
+
+    gJ = 2.0 * dn.T @ (YJ @ n)
+    gK = dn.T @ (YK @ n)
+    gK += blk(dfi, fi, S, W, YK) + blk(dfi, fi, W, S, YK) + blk(dfi, fi, W, W, YK)
+    gK += blk(dnd12, nd12, S, W, YK) - blk(dnd, nd, S, W, YK)
+    gK += blk(dnd12, nd12, W, S, YK) - blk(dnd, nd, W, S, YK)
+    gK += -blk(dnd12, nd12, W, W, YK) - blk(dnd, nd, W, W, YK)
+    # pair blocks G x G (strong first, then its weak orbitals): der_cjckd8
+    # overwrites them (C^J: 0; C^K: the sqrt forms) and calcoccg zeroes the
+    # diagonals; subtract the generic value computed above, add the actual
+    m = block.shape[1]
+    Gi = block[:, :, None]
+    Gj = block[:, None, :]
+    YJb, YKb = YJ[Gi, Gj], YK[Gi, Gj]  # (ndoc, m, m)
+    dnb = dn[block]  # (ndoc, m, nv)
+    nb_ = n[block]
+    gJ -= 2.0 * np.einsum("pak,pb,pab->k", dnb, nb_, YJb)
+    # generic C^K derivative in the block: base + the S x W, W x S, W x W terms
+    is_w = np.arange(m) > 0  # position 0 is the strong orbital (in S), the rest weak (in W)
+    sw = np.outer(~is_w, is_w) | np.outer(is_w, ~is_w)  # S x W or W x S
+    ww = np.outer(is_w, is_w)
+    gen = np.einsum("pak,pb->pabk", dnb, nb_)
+    fib, dfib = fi[block], dfi[block]
+    ndb, dndb, nd12b, dnd12b = nd[block], dnd[block], nd12[block], dnd12[block]
+    t_fi = np.einsum("pak,pb->pabk", dfib, fib)
+    t_12 = np.einsum("pak,pb->pabk", dnd12b, nd12b)
+    t_nd = np.einsum("pak,pb->pabk", dndb, ndb)
+    gen += (sw | ww)[None, :, :, None] * t_fi
+    gen += sw[None, :, :, None] * (t_12 - t_nd) + ww[None, :, :, None] * (-t_12 - t_nd)
+    gK -= np.einsum("pabk,pab->k", gen, YKb)
+    # actual C^K derivative in the block (der_cjckd8's intra-pair assignments)
+    sq = np.sqrt(nb_)
+    inv = 1.0 / np.sqrt(np.maximum(nb_, 1e-15))
+    act = np.zeros_like(gen)
+    act[:, 0, 1:, :] = 0.5 * inv[:, 0, None, None] * sq[:, 1:, None] * dnb[:, 0, None, :]
+    act[:, 1:, 0, :] = 0.5 * inv[:, 1:, None] * dnb[:, 1:, :] * sq[:, 0, None, None]
+    act[:, 1:, 1:, :] = -0.5 * (dnb[:, 1:, :] * inv[:, 1:, None])[:, :, None, :] * sq[:, None, 1:, None]
+    eye = np.eye(m, dtype=bool)
+    act[:, eye, :] = 0.0
+    gK += np.einsum("pabk,pab->k", act, YKb)
+    # diagonals outside the pair blocks (orbitals below no1: the reference's
+    # softmax writes pair i's strong row at index i), zeroed by calcoccg
+    out = np.ones(P, dtype=bool)
+    out[block.ravel()] = False
+    if np.any(out):
+        o = np.nonzero(out)[0]
+        gJ -= 2.0 * dn[o].T @ (n[o] * np.diagonal(YJ)[o])
+        gK -= dn[o].T @ (n[o] * np.diagonal(YK)[o])
+    g = dn.T @ (2.0 * H_core + np.diagonal(J_MO))
+    return g + 2.0 * gJ - 2.0 * gK
 
 
 def calcocce(gamma, J_MO, K_MO, H_core, p):

@@ -62,3 +62,23 @@ def test_orbital_gradient_rotation_ordering(case):
     Cs, gs = nof.order_occupations_softmax(g["C"], g["gamma"], p)
     assert nrel(Cs, g["C_sorted"]) < TOL
     assert np.allclose(gs, g["gamma_sorted"], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("nbf,ncwo,no1", [(24, 4, 0), (37, 3, 0), (60, 2, 0), (160, 4, 0), (40, 3, 2)])
+def test_calcoccg_fast_equals_dense(nbf, ncwo, no1):
+    """The contraction form of the occupation gradient equals calcoccg (the
+    dense restatement of pnof.py:1004-1033) on random J_MO, K_MO, H_core."""
+    from pynof_gb300 import nof, synthetic
+
+    st = synthetic.Structure(nbf=nbf, nbfaux=4 * nbf, ndoc=max(1, nbf // 10), ncwo=ncwo, no1=no1)
+    P = st.nbf5
+    rng = np.random.default_rng(nbf + ncwo)
+    A = rng.standard_normal((P, P))
+    J = A @ A.T / P + 0.01 * rng.standard_normal((P, P))
+    B = rng.standard_normal((P, P))
+    K = B @ B.T / P
+    Hc = rng.standard_normal(P)
+    g = nof.gamma_guess_softmax(st) + 0.5 * rng.standard_normal(st.nv)
+    a = nof.calcoccg(g, J, K, Hc, st)
+    b = nof.calcoccg_fast(g, J, K, Hc, st)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
