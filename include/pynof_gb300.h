@@ -216,6 +216,12 @@ size_t gb_rotate_orbital_workspace_f64(int nbf);
 int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double norm1, double* Cout,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* Plain FP64 GEMM C = A B^T with row-major A [M][K], B [N][K], C [M][N] on the
+ * DMMA engine (the FP64 counterpart of gb_dgemm_mixed).  No counterpart in
+ * the reference (numpy / cupy GEMMs); used e.g. for ERPA's (pq|sl) from b_pql
+ * (pynof/postpnof.py:1404-1406). */
+int gb_dgemm_f64(const double* A, const double* B, int M, int N, int K, double* C, void* stream);
+
 /* Capture of the calling thread's work on a (non-default) stream into a CUDA
  * graph, thread-local capture mode: gb_graph_begin, then any of this
  * library's calls that neither allocate nor synchronise (preallocated

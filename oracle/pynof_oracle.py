@@ -304,6 +304,14 @@ def mo4_full(C, I, p, q, r, t):
     return np.einsum("mp,nq,mnsl,sr,lt->pqrt", Cp, Cq, I, Cr, Ct, optimize=True)
 
 
+def erpa_mo_integrals_ri(C, H, b, P):
+    """``postpnof.py:1402-1406`` (RI): h and (pq|sl) from b_pql."""
+    Cp = C[:, :P]
+    h = np.einsum("mi,mn,nj->ij", Cp, H, Cp, optimize=True)
+    b_pql = np.einsum("mnl,mp,nq->pql", b, Cp, Cp, optimize=True)
+    return h, np.einsum("pqR,slR->pqsl", b_pql, b_pql, optimize=True)
+
+
 def eri_from_b(b):
     """(mn|sl) = sum_Q b[m, n, Q] b[s, l, Q] (the exact RI identity)."""
     N, _, Q = b.shape

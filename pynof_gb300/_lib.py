@@ -60,6 +60,7 @@ SIGNATURES = {
     "gb_energy_elec_workspace_f64": (_Z, [_I, _I]),
     "gb_energy_elec_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_ri_factor_f64": (_I, [_P, _P, _I, _I, _P, _P]),
+    "gb_dgemm_f64": (_I, [_P, _P, _I, _I, _I, _P, _P]),
     "gb_mo4_full_workspace_f64": (_Z, [_I, _I, _I, _I]),
     "gb_mo4_full_f64": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_graph_begin": (_I, [_P]),

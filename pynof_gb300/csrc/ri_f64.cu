@@ -327,3 +327,22 @@ extern "C" int gb_ri_factor_f64(const double* mnk, const double* M, int nbf, int
   return gemm_f64(g, static_cast<cudaStream_t>(stream));
 }
 
+// ---------------------------------------------------------------------------
+// Plain FP64 GEMM C = A B^T (row-major A [M][K], B [N][K], C [M][N]) on the
+// DMMA engine, the FP64 counterpart of gb_dgemm_mixed.
+// ---------------------------------------------------------------------------
+extern "C" int gb_dgemm_f64(const double* A, const double* B, int M, int N, int K, double* C, void* stream) {
+  clear_error();
+  GB_REQUIRE(M > 0 && N > 0 && K > 0, GB_ERR_BAD_SHAPE, "gb_dgemm_f64: bad sizes M=%d N=%d K=%d", M, N, K);
+  GB_REQUIRE(A && B && C, GB_ERR_INVALID_ARG, "gb_dgemm_f64: null pointer");
+  GemmF64 g{};
+  g.M = M; g.N = N; g.K = K; g.batch = 1;
+  g.A = {A, 0, lin(K), lin(1)};
+  g.B = {B, 0, lin(1), lin(K)};  // B(k, j) = B[j][k]
+  g.C = {C, 0, lin(N), lin(1)};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_NONE;
+  g.a_kfast = true; g.b_kfast = true;
+  g.tag = "gemm_f64:dgemm";
+  return gemm_f64(g, static_cast<cudaStream_t>(stream));
+}
+

@@ -195,3 +195,25 @@ def compute_b_mnl(mnk, metric, nslices: int | None = None, metric_is_power: bool
     Returns the device tensor (resident, as ``cp.array(b_mnl)`` at ``:53``)."""
     M = np.asarray(metric, dtype=np.float64) if metric_is_power else metric_power(metric)
     return ops.ri_factor(as_device(mnk), as_device(M), nslices)
+
+
+# ---------------------------------------------------------------------------
+# ERPA's MO integrals, RI route (postpnof.py:1402-1406, inline there)
+# ---------------------------------------------------------------------------
+def erpa_mo_integrals_ri(C, H, b_mnl, p):
+    """h = C_p^T H C_p (nbf5, nbf5) and (pq|sl) = sum_R b_pqR b_slR
+    (nbf5, nbf5, nbf5, nbf5) with b_pql = sum_mn C_mp C_nq b_mnl, p, q < nbf5
+    (``postpnof.py:1402-1406``), on the device: the MO transform of
+    computeLagrange2 (A5) and one GEMM over R, FP64 or split per ``PRECISION``.
+    Host numpy out (the reference ``.get()``s I)."""
+    P = p.nbf5
+    dC, dH, db = as_device(C), as_device(H), as_device(b_mnl)
+    Hmat, bMO = ops.mo_ri(dC, dH, db, P)
+    Q = bMO.shape[2]
+    bpq = bMO[:P].reshape(P * P, Q).contiguous()
+    if PRECISION["mode"] == "mixed":
+        I = ops.dgemm_mixed(bpq, bpq, PRECISION["nslices"])
+    else:
+        I = ops.dgemm_f64(bpq, bpq)
+    return to_host(Hmat[:P].contiguous(), I.view(P, P, P, P))
+

@@ -415,6 +415,19 @@ def dgemm_mixed(A: torch.Tensor, B: torch.Tensor, nslices: int = 6) -> torch.Ten
     return C
 
 
+def dgemm_f64(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """C = A B^T in FP64 on the DMMA engine."""
+    M, K = A.shape
+    N, K2 = B.shape
+    if K2 != K:
+        raise ValueError("A and B must share K")
+    _require(A, (M, K), "A")
+    _require(B, (N, K), "B")
+    C = torch.empty((M, N), dtype=_F64, device=A.device)
+    _lib.call("gb_dgemm_f64", _ptr(A), _ptr(B), M, N, K, _ptr(C), _stream(A.device))
+    return C
+
+
 class PreparedRI:
     """RI factor sliced for the tensor-core path (resident next to b)."""
 
