@@ -1214,8 +1214,11 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   GB_TRY(configure_device());
   const KArgs ka = make_args(A, B, g);
   const long long tiles = ozaki_tiles(g);
-  // outputs whose tile rows are the unit stride take the persistent kernel
-  const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1);
+  // outputs whose tile rows are the unit stride take the persistent kernel,
+  // unless pair symmetry skips whole row bands (the round-robin walk would
+  // then desynchronise the CTAs that share a block of the large operand)
+  const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1) &&
+                         g.sym != SYM_PAIRROW && g.sym != SYM_PAIRCOL;
   int dev = 0;
   cudaGetDevice(&dev);
   const int nsm = (dev >= 0 && dev < 64 && g_num_sms[dev] > 0) ? g_num_sms[dev] : 0;
