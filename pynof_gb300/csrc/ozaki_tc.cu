@@ -311,6 +311,33 @@ __device__ __forceinline__ bool decode_tile(const OzGemm& g, long long t, int& b
   return true;
 }
 
+// For a tile t that a pair symmetry skips: the end of the run of skipped
+// tiles that t starts (every tile in [t, end) is skipped).  The rows (or
+// columns) mm*n + nn with nn < mm that one block can lie in end at row
+// mm*n + mm, so the run ends at the block holding that row.
+template <int BN>
+__device__ __forceinline__ long long skip_run_end(const OzGemm& g, long long t) {
+  const int mtiles = (g.M + BM - 1) / BM;
+  const int ntiles = (g.N + BN - 1) / BN;
+  const long long per_batch = (long long)mtiles * ntiles;
+  const long long base = (t / per_batch) * per_batch;
+  const long long r = t % per_batch;
+  const bool m_fast = mtiles <= ntiles;  // the tile order of decode_tile
+  const int mi = m_fast ? (int)(r % mtiles) : (int)(r / ntiles);
+  const int ni = m_fast ? (int)(r / mtiles) : (int)(r % ntiles);
+  if (g.sym == SYM_PAIRROW) {
+    const long long ma = (long long)mi * BM / g.pair_n;
+    const long long b = (ma * g.pair_n + ma) / BM;
+    return base + (m_fast ? (long long)ni * mtiles + b : b * ntiles);
+  }
+  if (g.sym == SYM_PAIRCOL) {
+    const long long ma = (long long)ni * BN / g.pair_n;
+    const long long c = (ma * g.pair_n + ma) / BN;
+    return base + (m_fast ? c * mtiles : (long long)mi * ntiles + c);
+  }
+  return t + 1;
+}
+
 // One output tile, all roles.
 template <int S, int BN, int KIND>
 __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0, unsigned char* smem_raw) {
@@ -718,8 +745,12 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
 
 // Persistent form (bf16 digits; outputs whose tile rows are the unit stride,
 // so the epilogue stores straight from registers and never parks results in
-// the stage buffers).  One CTA per SM walks the tiles t = blockIdx.x,
-// + gridDim.x, ...  The producer runs ahead across tile boundaries (the next
+// the stage buffers).  One CTA per SM; its producer takes the tiles from a
+// counter in the caller's memory (so tiles start in order across the GPU, as
+// with the hardware's block dispatch, and the CTAs that share a block of the
+// large operand read it together) or, without one, walks t = blockIdx.x,
+// + gridDim.x, ...; it hands each tile index to the MMA issuer and the
+// epilogue through a small ring in shared memory.  The producer runs ahead across tile boundaries (the next
 // tile's first stages load during this tile's epilogue), and the epilogue
 // releases TMEM as soon as the last chunk is folded into registers, so the
 // next tile's MMAs overlap the conversion and stores.  Pipeline phases
@@ -744,6 +775,14 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + data_bytes + epi_table_bytes(BN));
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
+  // tile hand-off from the producer to the MMA issuer and the epilogue: a
+  // ring of tile indices (-1 ends the walk) behind full / empty barriers
+  constexpr int RING = 4;
+  static_assert(2 * STAGES + 6 <= 16 && (24 + RING / 2) * 8 <= 256, "barrier block of smem_bytes");
+  volatile int* ring = reinterpret_cast<volatile int*>(bars + 24);
+  const uint32_t ringbar0 = smem_u32(bars + 16);
+  auto ring_full = [&](int r) { return ringbar0 + 8u * r; };
+  auto ring_empty = [&](int r) { return ringbar0 + 8u * (RING + r); };
   const uint32_t sbase = smem_u32(smem);
   const uint32_t bar0 = smem_u32(bars);
   auto full_bar = [&](int st) { return bar0 + 8u * st; };
@@ -761,6 +800,10 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
     mbar_init(accfull_bar, 1);
     mbar_init(accempty_bar, NUM_EPI_WARPS);
     mbar_init(done_bar, 1);
+    for (int r = 0; r < RING; ++r) {
+      mbar_init(ring_full(r), 1);
+      mbar_init(ring_empty(r), 1 + NUM_EPI_WARPS);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -778,16 +821,44 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   const uint32_t tmem = *tmem_slot;
   const int nkb = (g.K + BK - 1) / BK;
   const int nchunks = (nkb + CH - 1) / CH;
-  const int tstep = gridDim.x;
 
   if (warp == 0) {
     // ---------------- producer ----------------
     if (lane == 0) {
       int gkb = 0;  // stages issued so far (all tiles)
       bool aborted = false;
-      for (int t = blockIdx.x; t < ntiles && !aborted; t += tstep) {
-        int bz, m0, n0;
-        if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
+      unsigned int next = blockIdx.x;  // static walk when no tile counter is given
+      for (int i = 0; !aborted; ++i) {
+        const int slot = i % RING;
+        if (!mbar_wait(ring_empty(slot), (uint32_t)(((i / RING) & 1) ^ 1), abort_flag)) {
+          signal_abort(abort_flag);
+          break;
+        }
+        // next tile that has work (tiles a symmetry skips are passed over here)
+        int t, bz, m0, n0;
+        for (;;) {
+          unsigned int u;
+          if (g.tile_counter) {
+            u = atomicAdd(g.tile_counter, 1u);
+          } else {
+            u = next;
+            next += gridDim.x;
+          }
+          if (u >= (unsigned int)ntiles) {
+            t = -1;
+            break;
+          }
+          t = (int)u;
+          if (decode_tile<BN>(g, t, bz, m0, n0)) break;
+          if (g.tile_counter) {
+            // move the counter past the rest of the skipped run at once
+            const long long e = skip_run_end<BN>(g, t);
+            if (e > (long long)u + 1) atomicMax(g.tile_counter, (unsigned int)e);
+          }
+        }
+        ring[slot] = t;
+        mbar_arrive(ring_full(slot));
+        if (t < 0) break;
         const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
         const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
                                   (long long)(m0 / BM) * a.A.kblocks() * a_bytes;
@@ -829,9 +900,17 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
     if (lane == 0) {
       int gkb = 0, gch = 0;
       bool aborted = false;
-      for (int t = blockIdx.x; t < ntiles && !aborted; t += tstep) {
+      for (int i = 0; !aborted; ++i) {
+        const int slot = i % RING;
+        if (!mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag)) {
+          signal_abort(abort_flag);
+          break;
+        }
+        const int t = ring[slot];
+        mbar_arrive(ring_empty(slot));
+        if (t < 0) break;
         int bz, m0, n0;
-        if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
+        decode_tile<BN>(g, t, bz, m0, n0);
         const int n_valid = min(BN, g.N - n0);
         const int n_mma = (n_valid + 15) & ~15;
         const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
@@ -891,11 +970,19 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
     const float upE = __int_as_float((127 + 7 * gE) << 23);
     const int row = q * 32 + lane;
     int gch = 0;
-    for (int t = blockIdx.x; t < ntiles; t += tstep) {
+    for (int i = 0;; ++i) {
+      const int slot = i % RING;
+      const bool got = mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag);
+      if (!got) signal_abort(abort_flag);
+      const int t = got ? ring[slot] : -1;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(ring_empty(slot));
+      // every epilogue warp is done with the previous tile's tables, and all
+      // of them take the same branch
+      if (epi_barrier_any(!got || *abort_flag != 0)) break;
+      if (t < 0) break;
       int bz, m0, n0;
-      if (!decode_tile<BN>(g, t, bz, m0, n0)) continue;
-      // every epilogue warp is done with the previous tile's tables
-      if (epi_barrier_any(*abort_flag != 0)) break;
+      decode_tile<BN>(g, t, bz, m0, n0);
       {
         const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
         if (et < BM) {
@@ -1214,22 +1301,31 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   GB_TRY(configure_device());
   const KArgs ka = make_args(A, B, g);
   const long long tiles = ozaki_tiles(g);
-  // outputs whose tile rows are the unit stride take the persistent kernel,
-  // unless pair symmetry skips whole row bands (the round-robin walk would
-  // then desynchronise the CTAs that share a block of the large operand)
+  // outputs whose tile rows are the unit stride take the persistent kernel;
+  // under pair symmetry (whole row bands skipped) only with the tile counter,
+  // as a static walk would desynchronise the CTAs that share a block of the
+  // large operand
   const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1) &&
-                         g.sym != SYM_PAIRROW && g.sym != SYM_PAIRCOL;
+                         ((g.sym != SYM_PAIRROW && g.sym != SYM_PAIRCOL) || g.tile_counter);
   int dev = 0;
   cudaGetDevice(&dev);
   const int nsm = (dev >= 0 && dev < 64 && g_num_sms[dev] > 0) ? g_num_sms[dev] : 0;
-  const int pi = prof_begin(g.tag, stream);
   if (g.S >= 1 && g.S <= 6 && g.bn == 128 && rows_fast && nsm > 0 && tiles < (1LL << 30)) {
     const long long grid = tiles < nsm ? tiles : nsm;
-    persistent_for(g.S)<<<(unsigned)grid, THREADS, smem_bytes(g.S, 128), stream>>>(ka, (int)tiles);
+    KArgs kp = ka;
+    if (g.tile_counter && tiles > grid) {
+      GB_TRY(cuda_status(cudaMemsetAsync(g.tile_counter, 0, sizeof(unsigned int), stream), "tile counter"));
+    } else {
+      kp.g.tile_counter = nullptr;  // one tile per CTA, or the static walk
+    }
+    const int pi = prof_begin(g.tag, stream);
+    persistent_for(g.S)<<<(unsigned)grid, THREADS, smem_bytes(g.S, 128), stream>>>(kp, (int)tiles);
+    prof_end(pi, stream);
   } else {
+    const int pi = prof_begin(g.tag, stream);
     kernel_for(g.S, g.bn)<<<grid_for(tiles), THREADS, smem_bytes(g.S, g.bn), stream>>>(ka);
+    prof_end(pi, stream);
   }
-  prof_end(pi, stream);
   const cudaError_t le = cudaGetLastError();
   if (le != cudaSuccess) return launch_error(g.tag, le, g.S, g.bn);
   return GB_OK;

@@ -36,6 +36,10 @@ struct OzGemm {
   // the MMAs; used for long contractions (K > 4096).
   int fdrain = 0;
   int bn = 128;  // N tile width: 32, 64 or 128 (128 required for SYM_ROWCOL)
+  // Device word (caller memory, zeroed here before each launch that uses it)
+  // from which the persistent form hands out tiles in order; null = a static
+  // round-robin walk.  Launches that share it must be ordered (one stream).
+  unsigned int* tile_counter = nullptr;
   const char* tag = "ozaki_tc";
 };
 

@@ -25,9 +25,11 @@ bool orbitals_on_n(long long P, long long rows) {
 }
 
 // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)] from the sliced C^T (A, rows q) and b (bT)
-int half_transform_gemm(const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q, double* Tf, cudaStream_t s) {
+int half_transform_gemm(const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q, double* Tf,
+                        unsigned int* ctr, cudaStream_t s) {
   OzGemm gt{};
   gt.K = N; gt.batch = 1; gt.S = A.code(); gt.C = Tf; gt.c_sb = 0; gt.sym = SYM_NONE; gt.tag = "ozaki_tc:half_transform";
+  gt.tile_counter = ctr;
   if (orbitals_on_n(P, (long long)N * Q)) {
     gt.M = N * Q; gt.N = P; gt.c_r = lin(1); gt.c_c = lin((long long)N * Q);
     return ozaki_gemm(bT, A, gt, s);
@@ -64,6 +66,7 @@ struct JkjMixedWs {
   SlicedDesc A, d, T;
   double* Tf;
   double* dv;
+  unsigned int* ctr;  // tile counter of the persistent GEMMs
 };
 
 template <class C>
@@ -73,12 +76,14 @@ void jkj_mixed_layout(C& c, int N, int P, int Q, int S, JkjMixedWs* w) {
   auto* dv = c.template take<double>((size_t)P * Q);
   SlicedDesc d = take_sliced(c, 1, P, Q, S);
   SlicedDesc T = take_sliced(c, P, N, Q, S);
+  auto* ctr = c.template take<unsigned int>(1);
   if (w) {
     w->A = A;
     w->Tf = tf;
     w->dv = dv;
     w->d = d;
     w->T = T;
+    w->ctr = ctr;
   }
 }
 
@@ -136,12 +141,13 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   // A rows q over K = m: element C[m][q]
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
   // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
-  GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, s));
+  GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, w.ctr, s));
   GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s));
   // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
   GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
   OzGemm gj{};
   gj.K = Q; gj.batch = 1; gj.S = S; gj.C = J; gj.c_sb = 0; gj.pair_n = N; gj.tag = "ozaki_tc:J";
+  gj.tile_counter = w.ctr;
   if (orbitals_on_n(P, (long long)N * N)) {
     gj.M = N * N; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_PAIRROW;
     GB_TRY(ozaki_gemm(pr.bJ, w.d, gj, s));
@@ -156,7 +162,7 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   // K_q is symmetric: the tile is stored transposed (rows on the unit stride),
   // which lets the epilogue store straight from its TMEM-lane layout
   gk.C = K; gk.c_sb = (long long)N * N; gk.c_r = lin(1); gk.c_c = lin(N);
-  gk.sym = SYM_ROWCOL; gk.tag = "ozaki_tc:K";
+  gk.sym = SYM_ROWCOL; gk.tag = "ozaki_tc:K"; gk.tile_counter = w.ctr;
   GB_TRY(ozaki_gemm(w.T, w.T, gk, s));
   return GB_OK;
 }
@@ -173,17 +179,19 @@ extern "C" int gb_device_status(int reset, int* status) {
 // ---------------------------------------------------------------------------
 namespace {
 template <class Cv>
-void dgemm_layout(Cv& c, int M, int N, int K, int S, SlicedDesc* a, SlicedDesc* b) {
+void dgemm_layout(Cv& c, int M, int N, int K, int S, SlicedDesc* a, SlicedDesc* b, unsigned int** ctr) {
   SlicedDesc sa = take_sliced(c, 1, M, K, S);
   SlicedDesc sb = take_sliced(c, 1, N, K, S);
+  auto* ct = c.template take<unsigned int>(1);
   if (a) *a = sa;
   if (b) *b = sb;
+  if (ctr) *ctr = ct;
 }
 }  // namespace
 
 extern "C" size_t gb_dgemm_mixed_workspace(int M, int N, int K, int nslices) {
   SizeCarve c;
-  dgemm_layout(c, M, N, K, nslices, nullptr, nullptr);
+  dgemm_layout(c, M, N, K, nslices, nullptr, nullptr, nullptr);
   return c.used;
 }
 
@@ -198,14 +206,15 @@ extern "C" int gb_dgemm_mixed(const double* A, const double* B, int M, int N, in
              "gb_dgemm_mixed: workspace too small");
   Carve wc(workspace, workspace_bytes);
   SlicedDesc sa, sb;
-  dgemm_layout(wc, M, N, K, nslices, &sa, &sb);
+  unsigned int* ctr = nullptr;
+  dgemm_layout(wc, M, N, K, nslices, &sa, &sb, &ctr);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   GB_TRY(slice_operand(SliceSrc{A, 0, lin(K), lin(1), true}, sa, s));
   GB_TRY(slice_operand(SliceSrc{B, 0, lin(K), lin(1), true}, sb, s));
   OzGemm g{};
   g.M = M; g.N = N; g.K = K; g.batch = 1; g.S = nslices;
   g.C = C; g.c_sb = 0; g.c_r = lin(N); g.c_c = lin(1);
-  g.sym = SYM_NONE; g.tag = "ozaki_tc:dgemm";
+  g.sym = SYM_NONE; g.tag = "ozaki_tc:dgemm"; g.tile_counter = ctr;
   return ozaki_gemm(sa, sb, g, s);
 }
 
@@ -219,6 +228,7 @@ namespace {
 struct JkhMixedWs {
   SlicedDesc A, Tt;
   double *Tf, *bpq, *d, *X;
+  unsigned int* ctr;  // tile counter of the persistent GEMMs
 };
 
 template <class Cv>
@@ -229,7 +239,8 @@ void jkh_mixed_layout(Cv& c, int N, int P, int Q, int S, JkhMixedWs* w) {
   auto* bpq = c.template take<double>((size_t)P * P * Q);
   auto* d = c.template take<double>((size_t)P * Q);
   auto* X = c.template take<double>((size_t)N * P);
-  if (w) *w = JkhMixedWs{A, Tt, tf, bpq, d, X};
+  auto* ctr = c.template take<unsigned int>(1);
+  if (w) *w = JkhMixedWs{A, Tt, tf, bpq, d, X, ctr};
 }
 
 // H_core[p] = C_p^T H C_p and (optionally) Hmat = C^T H C_p in FP64
@@ -256,9 +267,9 @@ int hcore_f64(const double* C, const double* H, int N, int P, double* X, double*
 }
 
 int half_transform_mixed(const double* C, const SlicedDesc& A, const SlicedDesc& bT, int N, int P, int Q,
-                         double* Tf, cudaStream_t s) {
+                         double* Tf, unsigned int* ctr, cudaStream_t s) {
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, A, s));
-  return half_transform_gemm(A, bT, N, P, Q, Tf, s);
+  return half_transform_gemm(A, bT, N, P, Q, Tf, ctr, s);
 }
 }  // namespace
 
@@ -284,11 +295,12 @@ extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* 
   JkhMixedWs w;
   jkh_mixed_layout(wc, N, P, Q, S, &w);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  GB_TRY(half_transform_mixed(C, w.A, pr.bT, N, P, Q, w.Tf, s));
+  GB_TRY(half_transform_mixed(C, w.A, pr.bT, N, P, Q, w.Tf, w.ctr, s));
   // T read with rows l and K = n: element T[p][n][l]
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
   OzGemm gq{};
   gq.K = N; gq.batch = P; gq.S = S; gq.C = w.bpq; gq.c_sb = (long long)P * Q; gq.sym = SYM_NONE; gq.tag = "ozaki_tc:bpq";
+  gq.tile_counter = w.ctr;
   if (orbitals_on_n(P, Q)) {
     gq.M = Q; gq.N = P; gq.c_r = lin(1); gq.c_c = lin(Q);
     GB_TRY(ozaki_gemm(w.Tt, w.A, gq, s));
@@ -322,6 +334,7 @@ struct Lag2MixedWs {
   double *Tf, *bMO, *Y, *X, *d, *w, *cjm;
   double* part;  // ns partial exchange products (ns > 1)
   int ns, kc;    // K splits of the exchange GEMM and K per split
+  unsigned int* ctr;  // tile counter of the persistent GEMMs
 };
 
 // K splits of the ck exchange GEMM (M = nbf, N = nbf5, K = nbf5 naux): with
@@ -365,7 +378,8 @@ void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
   auto* d = c.template take<double>((size_t)P * Q);
   auto* wv = c.template take<double>((size_t)P * Q);
   auto* cjm = c.template take<double>((size_t)P * P);
-  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, ns, kc};
+  auto* ctr = c.template take<unsigned int>(1);
+  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, ns, kc, ctr};
 }
 }  // namespace
 
@@ -401,13 +415,13 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Aall, s));
   SlicedDesc Ap = w.Aall;
   Ap.rows = P;
-  GB_TRY(half_transform_gemm(Ap, pr.bT, N, P, Q, w.Tf, s));
+  GB_TRY(half_transform_gemm(Ap, pr.bT, N, P, Q, w.Tf, w.ctr, s));
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
   // bMO[a][q][l] (batch q)
   OzGemm gm{};
   gm.M = N; gm.N = Q; gm.K = N; gm.batch = P; gm.S = S;
   gm.C = w.bMO; gm.c_sb = Q; gm.c_r = lin((long long)P * Q); gm.c_c = lin(1);
-  gm.sym = SYM_NONE; gm.tag = "ozaki_tc:bMO";
+  gm.sym = SYM_NONE; gm.tag = "ozaki_tc:bMO"; gm.tile_counter = w.ctr;
   GB_TRY(ozaki_gemm(w.Aall, w.Tt, gm, s));
   GB_TRY(hcore_f64(C, H, N, P, w.X, nullptr, Hmat, s));
   GB_TRY(launch_gather_diag(w.bMO, w.d, P, Q, (long long)P * Q + Q, s));
@@ -429,7 +443,7 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   GB_TRY(slice_operand(SliceSrc{w.Y, w.kc, lin((long long)P * Q), lin(1), true}, w.Sy, s));
   OzGemm ge{};
   ge.M = N; ge.N = P; ge.K = w.kc; ge.batch = w.ns; ge.S = S;
-  ge.sym = SYM_NONE; ge.negate = 1; ge.tag = "ozaki_tc:ck_exchange";
+  ge.sym = SYM_NONE; ge.negate = 1; ge.tag = "ozaki_tc:ck_exchange"; ge.tile_counter = w.ctr;
   if (w.ns > 1) {
     ge.C = w.part; ge.c_sb = (long long)N * P; ge.c_r = lin(P); ge.c_c = lin(1);
     GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
