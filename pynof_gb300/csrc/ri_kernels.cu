@@ -21,6 +21,37 @@ __global__ void contract_diag_kernel(const double* __restrict__ C, const double*
   d[(long long)q * Q + l] = acc;
 }
 
+// The same contraction, also recording the row exponents of T's digit
+// slicing with rows (q, n) and K = l: texps[q N + n] = E with
+// |T[q][n][l]| < 2^E for all l (entries preset below any E).  A warp holds 32
+// consecutive l; the exponent field's maximum over them comes from one warp
+// reduction per n and lands in lane n % 32, which folds it in with atomicMax
+// every 32 n.
+__global__ void contract_diag_exps_kernel(const double* __restrict__ C, const double* __restrict__ T,
+                                          double* __restrict__ d, int* __restrict__ texps, int N, int P, int Q) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y;
+  const int lane = threadIdx.x & 31;
+  const bool in = l < Q;  // the whole warp stays for the reductions
+  const double* Tq = T + (long long)q * N * Q + (in ? l : 0);
+  int* eq = texps + (long long)q * N;
+  double acc = 0.0;
+  unsigned int mine = 0;  // exponent field maximum of row n0 + lane
+  for (int n0 = 0; n0 < N; n0 += 32) {
+    const int nn = min(32, N - n0);
+    for (int j = 0; j < nn; ++j) {
+      const int n = n0 + j;
+      const double t = in ? __ldg(Tq + (long long)n * Q) : 0.0;
+      acc = fma(__ldg(C + (long long)n * N + q), t, acc);
+      const unsigned int ex = (unsigned int)((unsigned long long)__double_as_longlong(t) >> 52) & 0x7FFu;
+      const unsigned int mx = __reduce_max_sync(0xffffffffu, ex);
+      if (lane == j) mine = mx;
+    }
+    if (lane < nn) atomicMax(eq + n0 + lane, (int)(mine > 1u ? mine : 1u) - 1022);
+  }
+  if (in) d[(long long)q * Q + l] = acc;
+}
+
 __global__ void gather_diag_kernel(const double* __restrict__ src, double* __restrict__ d, int Q,
                                    long long stride_pp) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -115,7 +146,15 @@ inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) /
 
 }  // namespace
 
-int launch_contract_diag(const double* C, const double* T, double* d, int N, int P, int Q, cudaStream_t s) {
+int launch_contract_diag(const double* C, const double* T, double* d, int N, int P, int Q, cudaStream_t s,
+                         int* texps) {
+  if (texps) {
+    // every entry below any exponent folded in (0x80808080 < -1021)
+    GB_TRY(cuda_status(cudaMemsetAsync(texps, 0x80, sizeof(int) * (size_t)P * N, s), "contract_diag exponents"));
+    GB_LAUNCH("contract_diag", s,
+              contract_diag_exps_kernel<<<dim3(cdiv(Q, 128), P), 128, 0, s>>>(C, T, d, texps, N, P, Q));
+    return GB_OK;
+  }
   GB_LAUNCH("contract_diag", s, contract_diag_kernel<<<dim3(cdiv(Q, 128), P), 128, 0, s>>>(C, T, d, N, P, Q));
   return GB_OK;
 }

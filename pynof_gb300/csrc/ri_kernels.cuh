@@ -7,7 +7,10 @@
 namespace gb {
 
 // d[q][l] = sum_n C[n][q] T[q][n][l]
-int launch_contract_diag(const double* C, const double* T, double* d, int N, int P, int Q, cudaStream_t s);
+// d[q][l] = sum_n C[n][q] T[q][n][l]; with texps also the row exponents of
+// T's digit slicing with rows (q, n) and K = l (texps[q N + n]).
+int launch_contract_diag(const double* C, const double* T, double* d, int N, int P, int Q, cudaStream_t s,
+                         int* texps = nullptr);
 // d[p][l] = src[p * stride_pp + l]
 int launch_gather_diag(const double* src, double* d, int P, int Q, long long stride_pp, cudaStream_t s);
 // out[r] = sum_l src[r][l]^2

@@ -142,7 +142,8 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
   // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
   GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, w.ctr, s));
-  GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s));
+  // the contraction also records the row exponents of T's slicing below
+  GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s, w.T.kind == 0 ? w.T.exps : nullptr));
   // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
   GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
   OzGemm gj{};
@@ -156,7 +157,7 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
     GB_TRY(ozaki_gemm(w.d, pr.bJ, gj, s));
   }
   // K[q] = T_q T_q^T
-  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s));
+  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s, w.T.kind == 0));
   OzGemm gk{};
   gk.M = N; gk.N = N; gk.K = Q; gk.batch = P; gk.S = S;
   // K_q is symmetric: the tile is stored transposed (rows on the unit stride),

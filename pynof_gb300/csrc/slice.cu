@@ -200,14 +200,16 @@ inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) /
 
 }  // namespace
 
-int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s) {
+int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s, bool exps_ready) {
   GB_REQUIRE((dst.kind == 0 && dst.S >= 1 && dst.S <= 6) || (dst.kind == 1 && dst.S == 2), GB_ERR_INVALID_ARG,
              "slice_operand: bad split form (planes %d, kind %d)", dst.S, dst.kind);
   GB_REQUIRE(dst.batch >= 1 && dst.batch <= 65535 && dst.rows >= 0, GB_ERR_BAD_SHAPE, "slice_operand: bad batch");
   GB_REQUIRE((reinterpret_cast<uintptr_t>(dst.planes) & 15) == 0, GB_ERR_INVALID_ARG,
              "slice_operand: planes not 16-byte aligned");
   if (dst.rows == 0 || dst.K == 0) return GB_OK;
-  if (src.kfast) {
+  if (exps_ready) {
+    GB_REQUIRE(dst.kind == 0, GB_ERR_INVALID_ARG, "slice_operand: recorded exponents are for digit slices");
+  } else if (src.kfast) {
     GB_LAUNCH("slice_rowexp", s,
               rowexp_kfast_kernel<<<dim3(cdiv(dst.rows, 8), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K, dst.exps));
   } else {

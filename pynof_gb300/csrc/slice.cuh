@@ -90,7 +90,9 @@ SlicedDesc take_sliced(Cv& c, int batch, int rows, int K, int code) {
   return SlicedDesc{reinterpret_cast<__nv_bfloat16*>(p), e, batch, rows, K, f.S, f.kind};
 }
 
-// Exponents then digits; both kernels read the source once.
-int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s);
+// Exponents then digits; both kernels read the source once.  With
+// exps_ready the row exponents are already in dst.exps (recorded by the
+// kernel that wrote the source) and only the digits are formed.
+int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s, bool exps_ready = false);
 
 }  // namespace gb
