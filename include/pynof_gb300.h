@@ -277,6 +277,19 @@ size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
 int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
                     double* K, void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same build in two parts, so that a caller can copy J to the host while
+ * K is computed, and each range of K as soon as it is done (the drop-in
+ * JKj_RI_GPU does this with a second stream).  No counterpart in the
+ * reference, whose JKj_RI_GPU returns J and K from one call.
+ * gb_jkj_ri_mixed_j forms J and leaves T in the workspace (same size as for
+ * gb_jkj_ri_mixed); gb_jkj_ri_mixed_k then forms K[q] for q0 <= q < q1 from
+ * it, on the same stream and workspace.  Results are bitwise those of
+ * gb_jkj_ri_mixed. */
+int gb_jkj_ri_mixed_j(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
+                      void* workspace, size_t workspace_bytes, void* stream);
+int gb_jkj_ri_mixed_k(int nbf, int nbf5, int naux, int nslices, int q0, int q1, double* K, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
 /* A3  computeJKH_MO, RI, on the tensor cores (same outputs as gb_jkh_mo_ri_f64).
  *     Replaces JKH_MO_RI_GPU (pynof/integrals.py:383-399). */
 size_t gb_jkh_mo_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);

@@ -121,28 +121,17 @@ extern "C" size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nsl
   return c.used;
 }
 
-extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
-                               double* K, void* workspace, size_t workspace_bytes, void* stream) {
-  clear_error();
-  const int N = nbf, P = nbf5, Q = naux, S = nslices;
-  GB_TRY(check_mixed(N, P, Q, S));
-  GB_REQUIRE(C && prep && J && K, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed: null pointer");
-  GB_REQUIRE(workspace_bytes >= gb_jkj_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
-             "gb_jkj_ri_mixed: workspace too small (%zu < %zu)", workspace_bytes,
-             gb_jkj_ri_workspace_mixed(N, P, Q, S));
-  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
-  Prepared pr;
-  prepared_layout(pc, N, Q, S, &pr);
-  Carve wc(workspace, workspace_bytes);
-  JkjMixedWs w;
-  jkj_mixed_layout(wc, N, P, Q, S, &w);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-
+namespace {
+// The J half of the build: slices C^T, forms T (half transform), d and J.
+// Leaves T and the row exponents of its slicing in the workspace for
+// jkj_mixed_k.
+int jkj_mixed_j(const double* C, const Prepared& pr, const JkjMixedWs& w, int N, int P, int Q, int S, double* J,
+                cudaStream_t s) {
   // A rows q over K = m: element C[m][q]
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
   // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
   GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, w.ctr, s));
-  // the contraction also records the row exponents of T's slicing below
+  // the contraction also records the row exponents of T's slicing (jkj_mixed_k)
   GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s, w.T.kind == 0 ? w.T.exps : nullptr));
   // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
   GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
@@ -151,21 +140,84 @@ extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int n
   gj.tile_counter = w.ctr;
   if (orbitals_on_n(P, (long long)N * N)) {
     gj.M = N * N; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_PAIRROW;
-    GB_TRY(ozaki_gemm(pr.bJ, w.d, gj, s));
-  } else {
-    gj.M = P; gj.N = N * N; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_PAIRCOL;
-    GB_TRY(ozaki_gemm(w.d, pr.bJ, gj, s));
+    return ozaki_gemm(pr.bJ, w.d, gj, s);
   }
-  // K[q] = T_q T_q^T
-  GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(Q), lin(1), true}, w.T, s, w.T.kind == 0));
+  gj.M = P; gj.N = N * N; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_PAIRCOL;
+  return ozaki_gemm(w.d, pr.bJ, gj, s);
+}
+
+// The K half for orbitals q0 <= q < q1: K[q] = T_q T_q^T from the T that
+// jkj_mixed_j left in the workspace.
+int jkj_mixed_k(const JkjMixedWs& w, int N, int Q, int S, int q0, int q1, double* K, cudaStream_t s) {
+  if (q1 <= q0) return GB_OK;
+  SlicedDesc T = w.T;
+  T.planes = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<unsigned char*>(w.T.planes) +
+                                              (size_t)q0 * (size_t)w.T.batch_bytes());
+  T.exps = w.T.exps + (size_t)q0 * N;
+  T.batch = q1 - q0;
+  GB_TRY(slice_operand(SliceSrc{w.Tf + (size_t)q0 * N * Q, (long long)N * Q, lin(Q), lin(1), true}, T, s,
+                       T.kind == 0));
   OzGemm gk{};
-  gk.M = N; gk.N = N; gk.K = Q; gk.batch = P; gk.S = S;
+  gk.M = N; gk.N = N; gk.K = Q; gk.batch = q1 - q0; gk.S = S;
   // K_q is symmetric: the tile is stored transposed (rows on the unit stride),
   // which lets the epilogue store straight from its TMEM-lane layout
-  gk.C = K; gk.c_sb = (long long)N * N; gk.c_r = lin(1); gk.c_c = lin(N);
+  gk.C = K + (size_t)q0 * N * N; gk.c_sb = (long long)N * N; gk.c_r = lin(1); gk.c_c = lin(N);
   gk.sym = SYM_ROWCOL; gk.tag = "ozaki_tc:K"; gk.tile_counter = w.ctr;
-  GB_TRY(ozaki_gemm(w.T, w.T, gk, s));
+  return ozaki_gemm(T, T, gk, s);
+}
+
+int jkj_mixed_check(const char* who, int N, int P, int Q, int S, size_t workspace_bytes) {
+  GB_TRY(check_mixed(N, P, Q, S));
+  GB_REQUIRE(workspace_bytes >= gb_jkj_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "%s: workspace too small (%zu < %zu)", who, workspace_bytes, gb_jkj_ri_workspace_mixed(N, P, Q, S));
   return GB_OK;
+}
+}  // namespace
+
+extern "C" int gb_jkj_ri_mixed(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, double* J,
+                               double* K, void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(jkj_mixed_check("gb_jkj_ri_mixed", N, P, Q, S, workspace_bytes));
+  GB_REQUIRE(C && prep && J && K && workspace, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed: null pointer");
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GB_TRY(jkj_mixed_j(C, pr, w, N, P, Q, S, J, s));
+  return jkj_mixed_k(w, N, Q, S, 0, P, K, s);
+}
+
+extern "C" int gb_jkj_ri_mixed_j(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices,
+                                 double* J, void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(jkj_mixed_check("gb_jkj_ri_mixed_j", N, P, Q, S, workspace_bytes));
+  GB_REQUIRE(C && prep && J && workspace, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed_j: null pointer");
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  return jkj_mixed_j(C, pr, w, N, P, Q, S, J, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gb_jkj_ri_mixed_k(int nbf, int nbf5, int naux, int nslices, int q0, int q1, double* K,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(jkj_mixed_check("gb_jkj_ri_mixed_k", N, P, Q, S, workspace_bytes));
+  GB_REQUIRE(K && workspace, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed_k: null pointer");
+  GB_REQUIRE(0 <= q0 && q0 <= q1 && q1 <= P, GB_ERR_BAD_SHAPE, "gb_jkj_ri_mixed_k: need 0 <= q0 <= q1 <= nbf5 (%d, %d, %d)",
+             q0, q1, P);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  return jkj_mixed_k(w, N, Q, S, q0, q1, K, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int gb_device_status(int reset, int* status) {

@@ -110,7 +110,12 @@ def jkj_ri_device(C, b_mnl, nbf5):
 
 
 def JKj_RI_GPU(C, b_mnl, p):
-    """J, K (nbf5, nbf, nbf) -- ``pynof/integrals.py:234-245``."""
+    """J, K (nbf5, nbf, nbf) -- ``pynof/integrals.py:234-245``.  On the tensor
+    cores the copies to the host overlap the build (J while K is formed, K in
+    two ranges of orbitals)."""
+    if PRECISION["mode"] == "mixed":
+        db = as_device(b_mnl)
+        return ops.jkj_ri_mixed_host(as_device(C), prepared(db, PRECISION["nslices"]), p.nbf5)
     return to_host(*jkj_ri_device(C, b_mnl, p.nbf5))
 
 

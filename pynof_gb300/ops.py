@@ -457,6 +457,50 @@ def jkj_ri_mixed(C: torch.Tensor, prep: PreparedRI, nbf5: int):
     return J, K
 
 
+_COPY_STREAMS: dict = {}
+
+
+def _copy_stream(dev: torch.device) -> torch.cuda.Stream:
+    """A second stream per device for device-to-host copies."""
+    s = _COPY_STREAMS.get(dev)
+    if s is None:
+        s = _COPY_STREAMS[dev] = torch.cuda.Stream(device=dev)
+    return s
+
+
+def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int = 2):
+    """J, K (nbf5, nbf, nbf) as numpy arrays in pinned host memory, with the
+    device-to-host copies overlapped with the build: J is copied while K is
+    formed, and K in ``parts`` ranges of orbitals, each range as soon as it is
+    done (a second stream; ``gb_jkj_ri_mixed_j`` / ``gb_jkj_ri_mixed_k``).
+    Bitwise the results of :func:`jkj_ri_mixed`."""
+    N, Q, S = prep.nbf, prep.naux, prep.nslices
+    _require(C, (N, N), "C")
+    if parts < 1:
+        raise ValueError("parts must be >= 1")
+    dev = prep.device
+    J = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    K = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
+    Jh = torch.empty((nbf5, N, N), dtype=_F64, pin_memory=True)
+    Kh = torch.empty((nbf5, N, N), dtype=_F64, pin_memory=True)
+    wp, wn = _ws("gb_jkj_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
+    main, cs = torch.cuda.current_stream(dev), _copy_stream(dev)
+    _lib.call("gb_jkj_ri_mixed_j", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J), wp, wn, main.cuda_stream)
+    cs.wait_stream(main)
+    with torch.cuda.stream(cs):
+        Jh.copy_(J, non_blocking=True)
+    bounds = [nbf5 * i // parts for i in range(parts + 1)]
+    for q0, q1 in zip(bounds[:-1], bounds[1:]):
+        if q1 == q0:
+            continue
+        _lib.call("gb_jkj_ri_mixed_k", N, nbf5, Q, S, q0, q1, _ptr(K), wp, wn, main.cuda_stream)
+        cs.wait_stream(main)
+        with torch.cuda.stream(cs):
+            Kh[q0:q1].copy_(K[q0:q1], non_blocking=True)
+    cs.synchronize()
+    return Jh.numpy(), Kh.numpy()
+
+
 def jkh_mo_ri_mixed(C, H, prep: PreparedRI, nbf5: int, out=None):
     """J_MO, K_MO, H_core on the tensor cores (A3)."""
     N, Q, S = prep.nbf, prep.naux, prep.nslices

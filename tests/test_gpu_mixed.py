@@ -142,3 +142,34 @@ def test_jkh_mo_and_lagrange2_mixed_vs_oracle(torch_cuda):
         print(f"nslices={S}: J_MO {errs[0]:.2e} K_MO {errs[1]:.2e} elag {errs[2]:.2e}")
         assert max(errs) < tol, (S, errs)
         assert nrel(c.cpu().numpy(), cr) < 1e-12 and nrel(Hm.cpu().numpy(), Hr) < 1e-12
+
+
+@pytest.mark.parametrize("parts", [1, 2, 3, 7])
+def test_split_build_matches_one_call(torch_cuda, parts):
+    """J and K formed in two C-ABI calls (J, then K over ranges of orbitals),
+    copied to the host on a second stream, equal the one-call build bitwise."""
+    from pynof_gb300 import ops
+
+    N, P, Q = 96, 40, 180
+    rng = np.random.default_rng(parts)
+    b = rng.standard_normal((N, N, Q)) * 0.1
+    b = 0.5 * (b + b.transpose(1, 0, 2))
+    C, _ = np.linalg.qr(rng.standard_normal((N, N)))
+    db, dC = ops.to_device(b), ops.to_device(C)
+    prep = ops.PreparedRI(db, 6)
+    J, K = ops.jkj_ri_mixed(dC, prep, P)
+    Jh, Kh = ops.jkj_ri_mixed_host(dC, prep, P, parts=parts)
+    assert np.array_equal(Jh, J.cpu().numpy())
+    assert np.array_equal(Kh, K.cpu().numpy())
+
+
+def test_split_build_rejects_bad_range(torch_cuda):
+    from pynof_gb300 import _lib, ops
+
+    N, P, Q = 32, 10, 40
+    wp, wn = ops._ws("gb_jkj_ri_workspace_mixed", N, P, Q, 6, device=torch_cuda.device("cuda", 0))
+    K = torch_cuda.empty((P, N, N), dtype=torch_cuda.float64, device="cuda")
+    with pytest.raises(_lib.GBError):
+        _lib.call("gb_jkj_ri_mixed_k", N, P, Q, 6, 3, P + 1, K.data_ptr(), wp, wn, ops._stream())
+    with pytest.raises(_lib.GBError):
+        _lib.call("gb_jkj_ri_mixed_k", N, P, Q, 6, 5, 4, K.data_ptr(), wp, wn, ops._stream())
