@@ -216,6 +216,18 @@ size_t gb_rotate_orbital_workspace_f64(int nbf);
 int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, double norm1, double* Cout,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* A9  the occupation optimiser's function and gradient on the HOST (no GPU
+ * work, no stream): E(gamma) of calcocce (pynof/pnof.py:994-1001, via
+ * ocupacion_softmax, CJCKD8 and calce, pnof.py:770-809, 350-422, 905-929)
+ * and, when grad != NULL, dE/dgamma of calcoccg (pnof.py:1004-1033, with
+ * der_CJCKD8, pnof.py:425-525), in O(nbf5^2).  Closed shell without singly
+ * occupied orbitals: gamma [ndoc ncwo], J_MO and K_MO [nbf5][nbf5], H_core
+ * [nbf5], no1 + ndoc (1 + ncwo) <= nbf5.  Replaces the numpy evaluation that
+ * scipy's CG repeats thousands of times per occupation step
+ * (minimization.py:77-97). */
+int gb_occ_energy_grad_f64(const double* gamma, const double* J_MO, const double* K_MO, const double* H_core,
+                           int nbf5, int no1, int ndoc, int ncwo, double* energy, double* grad);
+
 /* Plain FP64 GEMM C = A B^T with row-major A [M][K], B [N][K], C [M][N] on the
  * DMMA engine (the FP64 counterpart of gb_dgemm_mixed).  No counterpart in
  * the reference (numpy / cupy GEMMs); used e.g. for ERPA's (pq|sl) from b_pql

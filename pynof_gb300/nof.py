@@ -282,6 +282,37 @@ def calcoccg_fast(gamma, J_MO, K_MO, H_core, p):
     return g + 2.0 * gJ - 2.0 * gK
 
 
+def native_occ_ok(p) -> bool:
+    """Structures the compiled occupation function covers (closed shell,
+    no singly occupied orbitals)."""
+    return p.MSpin == 0 and p.nsoc == 0 and p.ndoc >= 1 and p.ncwo >= 1
+
+
+class OccFunction:
+    """E(gamma) and dE/dgamma (calcocce, calcoccg) at fixed J_MO, K_MO,
+    H_core from the library's compiled host loop ``gb_occ_energy_grad_f64``:
+    one O(nbf5^2) pass instead of numpy's many small array operations.  A call
+    returns (E, g), the form ``scipy.optimize.minimize(..., jac=True)`` takes."""
+
+    def __init__(self, J_MO, K_MO, H_core, p):
+        from . import _lib
+
+        self._lib = _lib
+        self._J = np.ascontiguousarray(J_MO, dtype=np.float64)
+        self._K = np.ascontiguousarray(K_MO, dtype=np.float64)
+        self._H = np.ascontiguousarray(H_core, dtype=np.float64)
+        self._dims = (p.nbf5, p.no1, p.ndoc, p.ncwo)
+        self._E = np.zeros(1)
+        self._nv = p.nv
+
+    def __call__(self, gamma):
+        x = np.ascontiguousarray(gamma, dtype=np.float64)
+        g = np.empty(self._nv)
+        self._lib.call("gb_occ_energy_grad_f64", x.ctypes.data, self._J.ctypes.data, self._K.ctypes.data,
+                       self._H.ctypes.data, *self._dims, self._E.ctypes.data, g.ctypes.data)
+        return float(self._E[0]), g
+
+
 def calcocce(gamma, J_MO, K_MO, H_core, p):
     """``pnof.py:994-1001``."""
     n, _ = ocupacion_softmax(gamma, p)

@@ -218,8 +218,12 @@ def occoptr(gamma, C, be, p):
     J_MO, K_MO, H_core = be.jkh_mo(C)
     E, nit, success = 0.0, 0, True
     if p.ndoc > 0:
-        res = scipy.optimize.minimize(nof.calcocce, gamma, args=(J_MO, K_MO, H_core, p), jac=nof.calcoccg_fast,
-                                      method="CG")
+        if nof.native_occ_ok(p):
+            # the compiled E and dE/dgamma in one call (the same CG iterates)
+            res = scipy.optimize.minimize(nof.OccFunction(J_MO, K_MO, H_core, p), gamma, jac=True, method="CG")
+        else:
+            res = scipy.optimize.minimize(nof.calcocce, gamma, args=(J_MO, K_MO, H_core, p),
+                                          jac=nof.calcoccg_fast, method="CG")
         gamma, E, nit, success = res.x, res.fun, res.nit, res.success
     n, _ = nof.ocupacion_softmax(gamma, p)
     cj12, ck12 = nof.cjckd8(n, p)
@@ -305,7 +309,10 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
         C, gamma = nof.order_occupations_softmax(C, gamma, p)
         g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
         J_MO, K_MO, H_core = be.jkh_mo(C)
-        g_occ = np.linalg.norm(nof.calcoccg_fast(gamma, J_MO, K_MO, H_core, p))
+        if nof.native_occ_ok(p):
+            g_occ = np.linalg.norm(nof.OccFunction(J_MO, K_MO, H_core, p)(gamma)[1])
+        else:
+            g_occ = np.linalg.norm(nof.calcoccg_fast(gamma, J_MO, K_MO, H_core, p))
         for k, v in (("E_orb", E_orb), ("E_occ", E_occ), ("g_orb", g_orb), ("g_occ", g_occ), ("nit_orb", nit_orb),
                      ("nit_occ", nit_occ), ("precision", be.precision)):
             hist[k].append(v)
