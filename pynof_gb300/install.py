@@ -10,7 +10,7 @@ unchanged.  The dispatchers keep the reference's CPU branches for
 """
 from __future__ import annotations
 
-from . import integrals, integrals_full, integrals_hf, utils
+from . import integrals, integrals_full, integrals_hf, nof, utils
 
 #: (module attribute path in pynof, replacement) for the p.gpu branches
 GPU_FUNCTIONS = {
@@ -36,6 +36,30 @@ def _gpu_or_cpu(gpu_fn, cpu_fn):
     dispatch.__name__ = getattr(cpu_fn, "__name__", "dispatch")
     dispatch.__doc__ = f"p.gpu -> pynof_gb300, else the reference's {dispatch.__name__}"
     return dispatch
+
+
+def _occ_native(p) -> bool:
+    """GNOF (ipnof 8) with softmax occupations, closed shell: the structures
+    the compiled occupation function covers."""
+    return (getattr(p, "gpu", False) and getattr(p, "ipnof", None) == 8
+            and getattr(p, "occ_method", None) == "Softmax" and nof.native_occ_ok(p))
+
+
+def _occ_dispatch(cpu_fn, grad: bool):
+    """calcocce / calcoccg (pnof.py:994-1033), which occoptr hands to scipy's
+    minimize (minimization.py:84-86): the library's compiled host loop where
+    it applies, else the reference's own function."""
+
+    def fn(gamma, J_MO, K_MO, H_core, p):
+        if _occ_native(p):
+            f = nof.OccFunction(J_MO, K_MO, H_core, p)
+            return f(gamma)[1] if grad else f.energy(gamma)
+        return cpu_fn(gamma, J_MO, K_MO, H_core, p)
+
+    fn.__name__ = getattr(cpu_fn, "__name__", "calcoccg" if grad else "calcocce")
+    fn.__doc__ = (f"p.gpu, GNOF, softmax, closed shell -> the compiled occupation function, "
+                  f"else the reference's {fn.__name__}")
+    return fn
 
 
 def install(pynof) -> dict:
@@ -89,6 +113,15 @@ def install(pynof) -> dict:
         disp = _gpu_or_cpu(gpu_fn, cpu_fn)
         setattr(mod, name, disp)
         setattr(pynof, name, disp)
+    # the occupation optimiser's function and gradient (pnof.py:994-1033)
+    if hasattr(pynof, "pnof"):
+        for name, grad in (("calcocce", False), ("calcoccg", True)):
+            cpu_fn = getattr(pynof.pnof, name)
+            saved["pnof." + name] = cpu_fn
+            saved["pynof." + name] = getattr(pynof, name, cpu_fn)
+            disp = _occ_dispatch(cpu_fn, grad)
+            setattr(pynof.pnof, name, disp)
+            setattr(pynof, name, disp)
     return saved
 
 

@@ -312,6 +312,12 @@ class OccFunction:
                        self._H.ctypes.data, *self._dims, self._E.ctypes.data, g.ctypes.data)
         return float(self._E[0]), g
 
+    def energy(self, gamma) -> float:
+        x = np.ascontiguousarray(gamma, dtype=np.float64)
+        self._lib.call("gb_occ_energy_grad_f64", x.ctypes.data, self._J.ctypes.data, self._K.ctypes.data,
+                       self._H.ctypes.data, *self._dims, self._E.ctypes.data, None)
+        return float(self._E[0])
+
 
 def calcocce(gamma, J_MO, K_MO, H_core, p):
     """``pnof.py:994-1001``."""

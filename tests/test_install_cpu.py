@@ -29,7 +29,41 @@ def fake_pynof():
     pynof.rotate_orbital = pynof.utils.rotate_orbital
     pynof.integrals.compute_integrals = lambda wfn, mol, p: (1, 2, 3, 4, [], [], 7)
     pynof.compute_integrals = pynof.integrals.compute_integrals
+    pynof.pnof = types.ModuleType("pynof.pnof")
+    pynof.pnof.calcocce = lambda *a: ("reference", "calcocce")
+    pynof.pnof.calcoccg = lambda *a: ("reference", "calcoccg")
+    pynof.calcocce = pynof.pnof.calcocce
+    pynof.calcoccg = pynof.pnof.calcoccg
     return pynof
+
+
+def test_install_occupation_function():
+    """pynof.calcocce / calcoccg: the compiled loop for GNOF + softmax closed
+    shell on the device path, the reference's functions otherwise."""
+    import numpy as np
+
+    from pynof_gb300 import build, nof
+    from pynof_gb300.synthetic import Structure
+
+    build.build()
+    pynof = fake_pynof()
+    saved = inst.install(pynof)
+    st = Structure(nbf=24, nbfaux=96, ndoc=4, ncwo=3)
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((st.nbf5, st.nbf5))
+    J = A @ A.T
+    K = 0.5 * J
+    H = rng.standard_normal(st.nbf5)
+    gamma = rng.standard_normal(st.nv)
+    p = types.SimpleNamespace(**{**vars(st), "gpu": True, "ipnof": 8, "occ_method": "Softmax"})
+    assert abs(pynof.calcocce(gamma, J, K, H, p) - nof.calcocce(gamma, J, K, H, st)) < 1e-12 * abs(J).max()
+    assert np.abs(pynof.calcoccg(gamma, J, K, H, p) - nof.calcoccg(gamma, J, K, H, st)).max() < 1e-11 * abs(J).max()
+    for other in (dict(gpu=False), dict(ipnof=7), dict(occ_method="Trigonometric")):
+        q = types.SimpleNamespace(**{**vars(p), **other})
+        assert pynof.calcocce(gamma, J, K, H, q) == ("reference", "calcocce")
+        assert pynof.pnof.calcoccg(gamma, J, K, H, q) == ("reference", "calcoccg")
+    inst.uninstall(pynof, saved)
+    assert pynof.calcocce(gamma, J, K, H, p) == ("reference", "calcocce")
 
 
 def test_install_rebinds_and_restores():
