@@ -48,7 +48,7 @@ void mol_layout(Cv& c, int N, int P, int Q, int S, MolWs* w) {
 void prepared_views(const void* prep, int N, int Q, int S, SlicedDesc* bT, SlicedDesc* bJ) {
   Carve c(const_cast<void*>(prep), (size_t)-1);
   *bT = take_sliced(c, 1, N * Q, N, S);
-  *bJ = take_sliced(c, 1, N * N, Q, S);
+  *bJ = take_sliced(c, 1, N * (N + 1) / 2, Q, S);  // the pairs m <= n (the prepared layout)
 }
 
 int bn_of(int code) { return code == 1 ? 32 : code == 2 ? 64 : 128; }
@@ -110,12 +110,12 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
     tilesT += ozaki_tiles(pt[i].g);
     OzGemm h{};
     h.S = S; h.batch = 1; h.c_sb = 0; h.pair_n = N; h.K = Q;
-    if (jcfg == 0) {  // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
-      h.M = P; h.N = N * N; h.bn = 128; h.sym = SYM_PAIRCOL;
+    if (jcfg == 0) {  // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l], pairs m <= n, mirrored
+      h.M = P; h.N = N * (N + 1) / 2; h.bn = 128; h.sym = SYM_TRICOL;
       h.C = J[i]; h.c_r = lin((long long)N * N); h.c_c = lin(1);
       pj[i] = OzProblem{w.d, bJ, h};
     } else {
-      h.M = N * N; h.N = P; h.bn = bn_of(jcfg); h.sym = SYM_PAIRROW;
+      h.M = N * (N + 1) / 2; h.N = P; h.bn = bn_of(jcfg); h.sym = SYM_TRIROW;
       h.C = J[i]; h.c_r = lin(1); h.c_c = lin((long long)N * N);
       pj[i] = OzProblem{bJ, w.d, h};
     }

@@ -41,7 +41,23 @@ struct OutF64 {
 
 // SYM_PAIRROW (tensor-core path only): rows encode the pair i = m * pair_n + n,
 // tiles whose rows all have n < m are skipped, rows with n > m are mirrored.
-enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2, SYM_PAIRROW = 3 };
+// SYM_TRIROW / SYM_TRICOL (tensor-core path only): rows (columns) are the
+// packed upper triangle of the pairs, r -> (m, n) with m <= n (tri_pair),
+// pair_n (pair_n + 1) / 2 of them; the output at pair m * pair_n + n is
+// written, and for n > m also its mirror n * pair_n + m.
+enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2, SYM_PAIRROW = 3, SYM_TRIROW = 4, SYM_TRICOL = 5 };
+
+// Packed upper-triangle index r = m N - m (m - 1) / 2 + (n - m), 0 <= m <= n < N,
+// back to (m, n) (rows of the triangle in order, each from its diagonal on).
+__host__ __device__ __forceinline__ void tri_pair(long long r, int N, int& m, int& n) {
+  const double b = 2.0 * N + 1.0;
+  long long x = (long long)((b - sqrt(b * b - 8.0 * (double)r)) * 0.5);
+  x = x < 0 ? 0 : (x > N - 1 ? N - 1 : x);
+  while (x > 0 && x * N - x * (x - 1) / 2 > r) --x;
+  while (x + 1 < N && (x + 1) * N - (x + 1) * x / 2 <= r) ++x;
+  m = (int)x;
+  n = (int)(r - (x * N - x * (x - 1) / 2) + x);
+}
 
 struct GemmF64 {
   int M, N, K, batch;

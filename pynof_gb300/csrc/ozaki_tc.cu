@@ -531,7 +531,14 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
           const int mm = i / g.pair_n, nn = i % g.pair_n;  // the mirrored row of a pair-symmetric row
           if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
         }
-        e_roff[et] = in ? g.c_r.at(i) : 0;
+        long long ri = i;  // the pair's index for a packed-triangle row
+        if (in && g.sym == SYM_TRIROW) {
+          int mm, nn;
+          tri_pair(i, g.pair_n, mm, nn);
+          ri = (long long)mm * g.pair_n + nn;
+          if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
+        }
+        e_roff[et] = in ? g.c_r.at(ri) : 0;
         e_mr[et] = mr;
         e_srow[et] = in ? a.A.exps[abz * g.M + i] : 0;
       } else if (et < BM + BN) {
@@ -543,7 +550,14 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
           const int mm = jj / g.pair_n, nn = jj % g.pair_n;
           if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
         }
-        e_coff[c] = in ? g.c_c.at(jj) : 0;
+        long long cj = jj;
+        if (in && g.sym == SYM_TRICOL) {
+          int mm, nn;
+          tri_pair(jj, g.pair_n, mm, nn);
+          cj = (long long)mm * g.pair_n + nn;
+          if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
+        }
+        e_coff[c] = in ? g.c_c.at(cj) : 0;
         e_mc[c] = mc;
         e_scol[c] = in ? a.B.exps[bbz * g.N + jj] - (KIND ? 31 : 7 * gE + a.frac) : 0;
       }
@@ -646,9 +660,9 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         Cb[ro + co] = val;
         if (mirror_rc) {
           Cb[mc + mr] = val;
-        } else if (g.sym == SYM_PAIRCOL) {
+        } else if (g.sym == SYM_PAIRCOL || g.sym == SYM_TRICOL) {
           if (mc >= 0) Cb[ro + mc] = val;
-        } else if (g.sym == SYM_PAIRROW) {
+        } else if (g.sym == SYM_PAIRROW || g.sym == SYM_TRIROW) {
           if (mr >= 0) Cb[mr + co] = val;
         }
       };
@@ -994,7 +1008,14 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
             const int mm = i / g.pair_n, nn = i % g.pair_n;
             if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
           }
-          e_roff[et] = in ? g.c_r.at(i) : 0;
+          long long ri = i;  // the pair's index for a packed-triangle row
+          if (in && g.sym == SYM_TRIROW) {
+            int mm, nn;
+            tri_pair(i, g.pair_n, mm, nn);
+            ri = (long long)mm * g.pair_n + nn;
+            if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
+          }
+          e_roff[et] = in ? g.c_r.at(ri) : 0;
           e_mr[et] = mr;
           e_srow[et] = in ? a.A.exps[abz * g.M + i] : 0;
         } else if (et < BM + BN) {
@@ -1006,7 +1027,14 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
             const int mm = jj / g.pair_n, nn = jj % g.pair_n;
             if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
           }
-          e_coff[c] = in ? g.c_c.at(jj) : 0;
+          long long cj = jj;
+          if (in && g.sym == SYM_TRICOL) {
+            int mm, nn;
+            tri_pair(jj, g.pair_n, mm, nn);
+            cj = (long long)mm * g.pair_n + nn;
+            if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
+          }
+          e_coff[c] = in ? g.c_c.at(cj) : 0;
           e_mc[c] = mc;
           e_scol[c] = in ? a.B.exps[bbz * g.N + jj] - 7 * gE - a.frac : 0;
         }
@@ -1090,10 +1118,10 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           Cb[ro + co] = val;
           if (mirror_rc) {
             Cb[e_mc[c] + mr] = val;
-          } else if (g.sym == SYM_PAIRCOL) {
+          } else if (g.sym == SYM_PAIRCOL || g.sym == SYM_TRICOL) {
             const long long mc = e_mc[c];
             if (mc >= 0) Cb[ro + mc] = val;
-          } else if (g.sym == SYM_PAIRROW) {
+          } else if (g.sym == SYM_PAIRROW || g.sym == SYM_TRIROW) {
             if (mr >= 0) Cb[mr + co] = val;
           }
         }
@@ -1263,6 +1291,10 @@ int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
              "ozaki_gemm: SYM_PAIRCOL needs N == pair_n^2");
   GB_REQUIRE(g.sym != SYM_PAIRROW || (long long)g.pair_n * g.pair_n == g.M, GB_ERR_BAD_SHAPE,
              "ozaki_gemm: SYM_PAIRROW needs M == pair_n^2");
+  GB_REQUIRE(g.sym != SYM_TRIROW || (long long)g.pair_n * (g.pair_n + 1) / 2 == g.M, GB_ERR_BAD_SHAPE,
+             "ozaki_gemm: SYM_TRIROW needs M == pair_n (pair_n + 1) / 2");
+  GB_REQUIRE(g.sym != SYM_TRICOL || (long long)g.pair_n * (g.pair_n + 1) / 2 == g.N, GB_ERR_BAD_SHAPE,
+             "ozaki_gemm: SYM_TRICOL needs N == pair_n (pair_n + 1) / 2");
   GB_REQUIRE(g.K > 0 && g.batch <= 65535, GB_ERR_BAD_SHAPE, "ozaki_gemm: bad K or batch");
   GB_REQUIRE((reinterpret_cast<uintptr_t>(A.planes) & 15) == 0 && (reinterpret_cast<uintptr_t>(B.planes) & 15) == 0,
              GB_ERR_INVALID_ARG, "ozaki_gemm: slice planes not 16-byte aligned");

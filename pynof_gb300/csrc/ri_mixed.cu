@@ -3,7 +3,9 @@
 //
 // The RI factor is sliced once ("prepared") into two K-major digit copies:
 //   bT[j = (n, l)][m]  (K = m, for the half transform T = C_p^T b)
-//   bJ[j = (m, n)][l]  (K = l, for J = d b^T)
+//   bJ[r = (m, n), m <= n][l]  (K = l, for J = d b^T; b and J_q are symmetric
+//                      in (m, n), so only the packed upper triangle of the
+//                      pairs is kept and J's GEMM writes each pair twice)
 // and stays resident across builds, like b itself in PyNOF's GPU path.
 #include "gemm_f64.cuh"
 #include "ozaki_tc.cuh"
@@ -45,7 +47,7 @@ struct Prepared {
 template <class C>
 void prepared_layout(C& c, int N, int Q, int S, Prepared* out) {
   SlicedDesc t = take_sliced(c, 1, N * Q, N, S);
-  SlicedDesc j = take_sliced(c, 1, N * N, Q, S);
+  SlicedDesc j = take_sliced(c, 1, N * (N + 1) / 2, Q, S);
   if (out) {
     out->bT = t;
     out->bJ = j;
@@ -110,8 +112,8 @@ extern "C" int gb_ri_prepare_mixed(const double* b, int nbf, int naux, int nslic
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // bT rows j = n*Q + l over K = m: element b[m][j]   (rows are the unit stride)
   GB_TRY(slice_operand(SliceSrc{b, 0, lin(1), lin((long long)N * Q), false}, pr.bT, s));
-  // bJ rows j = m*N + n over K = l: element b[j][l]  (K is the unit stride)
-  GB_TRY(slice_operand(SliceSrc{b, 0, lin(Q), lin(1), true}, pr.bJ, s));
+  // bJ rows r = (m, n), m <= n, over K = l: element b[m*N + n][l]  (K is the unit stride)
+  GB_TRY(slice_operand(SliceSrc{b, 0, lin(Q), lin(1), true, N}, pr.bJ, s));
   return GB_OK;
 }
 
@@ -135,14 +137,16 @@ int jkj_mixed_j(const double* C, const Prepared& pr, const JkjMixedWs& w, int N,
   GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s, w.T.kind == 0 ? w.T.exps : nullptr));
   // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
   GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
+  // (bJ's rows are the pairs m <= n; each result is also written to (n, m))
   OzGemm gj{};
   gj.K = Q; gj.batch = 1; gj.S = S; gj.C = J; gj.c_sb = 0; gj.pair_n = N; gj.tag = "ozaki_tc:J";
   gj.tile_counter = w.ctr;
-  if (orbitals_on_n(P, (long long)N * N)) {
-    gj.M = N * N; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_PAIRROW;
+  const int npairs = N * (N + 1) / 2;
+  if (orbitals_on_n(P, npairs)) {
+    gj.M = npairs; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_TRIROW;
     return ozaki_gemm(pr.bJ, w.d, gj, s);
   }
-  gj.M = P; gj.N = N * N; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_PAIRCOL;
+  gj.M = P; gj.N = npairs; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_TRICOL;
   return ozaki_gemm(w.d, pr.bJ, gj, s);
 }
 

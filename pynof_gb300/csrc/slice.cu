@@ -47,7 +47,7 @@ __global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restri
   const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
-  const double* base = src.p + b * src.sb + src.r.at(row);
+  const double* base = src.p + b * src.sb + src.row_at(row);
   unsigned long long mx = 0;
   for (int k = lane; k < K; k += 32) {
     const unsigned long long v = abs_bits(base[src.k.at(k)]);
@@ -66,7 +66,7 @@ __global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restri
   const long long b = blockIdx.y;
   const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= rows) return;
-  const double* base = src.p + b * src.sb + src.r.at(row);
+  const double* base = src.p + b * src.sb + src.row_at(row);
   unsigned long long mx = 0;
   for (int k = 0; k < K; ++k) {
     const unsigned long long v = abs_bits(base[src.k.at(k)]);
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) digits_blocked_kernel(SliceSrc src, Slice
   const int k0 = kb * SL_K + kg * 8;
   unsigned short dg[8][S];
   const bool rok = r < dst.rows;
-  const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
+  const double* base = src.p + b * src.sb + (rok ? src.row_at(r) : 0);
   const int e = rok ? dst.exps[b * dst.rows + r] : 0;
   double xs[8];
   const double* p8 = base + k0;
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256) tf32_blocked_kernel(SliceSrc src, SlicedD
   const int r = rb * SL_ROWS + rg * 8 + ri;
   const int k0 = kb * (SL_K / 2) + kg * 4;
   const bool rok = r < dst.rows;
-  const double* base = src.p + b * src.sb + (rok ? src.r.at(r) : 0);
+  const double* base = src.p + b * src.sb + (rok ? src.row_at(r) : 0);
   const int e = rok ? dst.exps[b * dst.rows + r] : 0;
   uint32_t hi[4], lo[4];
 #pragma unroll

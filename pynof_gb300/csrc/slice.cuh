@@ -58,6 +58,15 @@ struct SliceSrc {
   long long sb;  // batch stride
   Index2 r, k;   // row and K index maps
   bool kfast;    // K is the unit-stride index (else rows are)
+  // > 0: the rows are the packed upper triangle of tri_n x tri_n index
+  // pairs (tri_pair); row r reads r.at(m * tri_n + n)
+  int tri_n = 0;
+  __host__ __device__ __forceinline__ long long row_at(long long row) const {
+    if (tri_n <= 0) return r.at(row);
+    int m, n;
+    tri_pair(row, tri_n, m, n);
+    return r.at((long long)m * tri_n + n);
+  }
 };
 
 struct SlicedDesc {

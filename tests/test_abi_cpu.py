@@ -53,7 +53,9 @@ def test_workspace_queries(lib):
 
 def test_split_codes(lib):
     """GB_SPLIT_TF32X3 in the header is ops.SPLIT_TF32X3, and its prepared
-    factor (two 32-bit planes) is smaller than six bf16 digit planes."""
+    factor (two 32-bit planes of b's half-transform copy, N Q rows x N, and of
+    its pair copy, the N (N + 1) / 2 pairs m <= n x Q) is smaller than six
+    bf16 digit planes."""
     from pynof_gb300 import _lib, ops
 
     hdr = open(HEADER).read()
@@ -62,7 +64,7 @@ def test_split_codes(lib):
     N, Q = 600, 2400
     tf = _lib.query("gb_ri_prepare_bytes_mixed", N, Q, ops.SPLIT_TF32X3)
     s6 = _lib.query("gb_ri_prepare_bytes_mixed", N, Q, 6)
-    assert 2 * N * N * Q * 8 <= tf < s6
+    assert 8 * (N * Q * N + N * (N + 1) // 2 * Q) <= tf < s6
 
 
 def test_version_and_error(lib):
