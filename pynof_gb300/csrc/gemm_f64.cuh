@@ -39,13 +39,12 @@ struct OutF64 {
   Index2 r, c;
 };
 
-// SYM_PAIRROW (tensor-core path only): rows encode the pair i = m * pair_n + n,
-// tiles whose rows all have n < m are skipped, rows with n > m are mirrored.
-// SYM_TRIROW / SYM_TRICOL (tensor-core path only): rows (columns) are the
-// packed upper triangle of the pairs, r -> (m, n) with m <= n (tri_pair),
-// pair_n (pair_n + 1) / 2 of them; the output at pair m * pair_n + n is
-// written, and for n > m also its mirror n * pair_n + m.
-enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2, SYM_PAIRROW = 3, SYM_TRIROW = 4, SYM_TRICOL = 5 };
+// SYM_TRIROW / SYM_TRICOL (tensor-core path only, where they replace
+// SYM_PAIRCOL): rows (columns) are the packed upper triangle of the pairs,
+// r -> (m, n) with m <= n (tri_pair), pair_n (pair_n + 1) / 2 of them; the
+// output at pair m * pair_n + n is written, and for n > m also its mirror
+// n * pair_n + m.
+enum SymMode { SYM_NONE = 0, SYM_ROWCOL = 1, SYM_PAIRCOL = 2, SYM_TRIROW = 4, SYM_TRICOL = 5 };
 
 // Packed upper-triangle index r = m N - m (m - 1) / 2 + (n - m), 0 <= m <= n < N,
 // back to (m, n) (rows of the triangle in order, each from its diagonal on).

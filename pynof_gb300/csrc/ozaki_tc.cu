@@ -297,45 +297,7 @@ __device__ __forceinline__ bool decode_tile(const OzGemm& g, long long t, int& b
     n0 = (int)(r % ntiles) * BN;
     m0 = (int)(r / ntiles) * BM;
   }
-  if (g.sym == SYM_ROWCOL && m0 > n0) return false;
-  if (g.sym == SYM_PAIRCOL) {
-    const int j1 = min(n0 + BN, g.N) - 1;
-    const int ma = n0 / g.pair_n, mb = j1 / g.pair_n;
-    if (ma == mb && (j1 % g.pair_n) < ma) return false;
-  }
-  if (g.sym == SYM_PAIRROW) {
-    const int i1 = min(m0 + BM, g.M) - 1;
-    const int ma = m0 / g.pair_n, mb = i1 / g.pair_n;
-    if (ma == mb && (i1 % g.pair_n) < ma) return false;
-  }
-  return true;
-}
-
-// For a tile t that a pair symmetry skips: the end of the run of skipped
-// tiles that t starts (every tile in [t, end) is skipped).  The rows (or
-// columns) mm*n + nn with nn < mm that one block can lie in end at row
-// mm*n + mm, so the run ends at the block holding that row.
-template <int BN>
-__device__ __forceinline__ long long skip_run_end(const OzGemm& g, long long t) {
-  const int mtiles = (g.M + BM - 1) / BM;
-  const int ntiles = (g.N + BN - 1) / BN;
-  const long long per_batch = (long long)mtiles * ntiles;
-  const long long base = (t / per_batch) * per_batch;
-  const long long r = t % per_batch;
-  const bool m_fast = mtiles <= ntiles;  // the tile order of decode_tile
-  const int mi = m_fast ? (int)(r % mtiles) : (int)(r / ntiles);
-  const int ni = m_fast ? (int)(r / mtiles) : (int)(r % ntiles);
-  if (g.sym == SYM_PAIRROW) {
-    const long long ma = (long long)mi * BM / g.pair_n;
-    const long long b = (ma * g.pair_n + ma) / BM;
-    return base + (m_fast ? (long long)ni * mtiles + b : b * ntiles);
-  }
-  if (g.sym == SYM_PAIRCOL) {
-    const long long ma = (long long)ni * BN / g.pair_n;
-    const long long c = (ma * g.pair_n + ma) / BN;
-    return base + (m_fast ? c * mtiles : (long long)mi * ntiles + c);
-  }
-  return t + 1;
+  return !(g.sym == SYM_ROWCOL && m0 > n0);
 }
 
 // One output tile, all roles.
@@ -527,10 +489,6 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         const bool in = i < g.M;
         long long mr = -1;
         if (in && g.sym == SYM_ROWCOL) mr = g.c_c.at(i);
-        if (in && g.sym == SYM_PAIRROW) {
-          const int mm = i / g.pair_n, nn = i % g.pair_n;  // the mirrored row of a pair-symmetric row
-          if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
-        }
         long long ri = i;  // the pair's index for a packed-triangle row
         if (in && g.sym == SYM_TRIROW) {
           int mm, nn;
@@ -546,10 +504,6 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         const bool in = jj < g.N;
         long long mc = -1;
         if (in && g.sym == SYM_ROWCOL) mc = g.c_r.at(jj);
-        if (in && g.sym == SYM_PAIRCOL) {
-          const int mm = jj / g.pair_n, nn = jj % g.pair_n;
-          if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
-        }
         long long cj = jj;
         if (in && g.sym == SYM_TRICOL) {
           int mm, nn;
@@ -660,9 +614,9 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         Cb[ro + co] = val;
         if (mirror_rc) {
           Cb[mc + mr] = val;
-        } else if (g.sym == SYM_PAIRCOL || g.sym == SYM_TRICOL) {
+        } else if (g.sym == SYM_TRICOL) {
           if (mc >= 0) Cb[ro + mc] = val;
-        } else if (g.sym == SYM_PAIRROW || g.sym == SYM_TRIROW) {
+        } else if (g.sym == SYM_TRIROW) {
           if (mr >= 0) Cb[mr + co] = val;
         }
       };
@@ -864,11 +818,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           }
           t = (int)u;
           if (decode_tile<BN>(g, t, bz, m0, n0)) break;
-          if (g.tile_counter) {
-            // move the counter past the rest of the skipped run at once
-            const long long e = skip_run_end<BN>(g, t);
-            if (e > (long long)u + 1) atomicMax(g.tile_counter, (unsigned int)e);
-          }
         }
         ring[slot] = t;
         mbar_arrive(ring_full(slot));
@@ -1004,10 +953,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           const bool in = i < g.M;
           long long mr = -1;
           if (in && g.sym == SYM_ROWCOL) mr = g.c_c.at(i);
-          if (in && g.sym == SYM_PAIRROW) {
-            const int mm = i / g.pair_n, nn = i % g.pair_n;
-            if (nn > mm) mr = g.c_r.at((long long)nn * g.pair_n + mm);
-          }
           long long ri = i;  // the pair's index for a packed-triangle row
           if (in && g.sym == SYM_TRIROW) {
             int mm, nn;
@@ -1023,10 +968,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           const bool in = jj < g.N;
           long long mc = -1;
           if (in && g.sym == SYM_ROWCOL) mc = g.c_r.at(jj);
-          if (in && g.sym == SYM_PAIRCOL) {
-            const int mm = jj / g.pair_n, nn = jj % g.pair_n;
-            if (nn > mm) mc = g.c_c.at((long long)nn * g.pair_n + mm);
-          }
           long long cj = jj;
           if (in && g.sym == SYM_TRICOL) {
             int mm, nn;
@@ -1118,10 +1059,10 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           Cb[ro + co] = val;
           if (mirror_rc) {
             Cb[e_mc[c] + mr] = val;
-          } else if (g.sym == SYM_PAIRCOL || g.sym == SYM_TRICOL) {
+          } else if (g.sym == SYM_TRICOL) {
             const long long mc = e_mc[c];
             if (mc >= 0) Cb[ro + mc] = val;
-          } else if (g.sym == SYM_PAIRROW || g.sym == SYM_TRIROW) {
+          } else if (g.sym == SYM_TRIROW) {
             if (mr >= 0) Cb[mr + co] = val;
           }
         }
@@ -1287,10 +1228,8 @@ int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
              GB_ERR_BAD_SHAPE, "ozaki_gemm: operand shapes do not match the GEMM");
   GB_REQUIRE(g.sym != SYM_ROWCOL || (g.M == g.N && g.bn == BM), GB_ERR_BAD_SHAPE,
              "ozaki_gemm: SYM_ROWCOL needs M == N and 128-wide tiles");
-  GB_REQUIRE(g.sym != SYM_PAIRCOL || (long long)g.pair_n * g.pair_n == g.N, GB_ERR_BAD_SHAPE,
-             "ozaki_gemm: SYM_PAIRCOL needs N == pair_n^2");
-  GB_REQUIRE(g.sym != SYM_PAIRROW || (long long)g.pair_n * g.pair_n == g.M, GB_ERR_BAD_SHAPE,
-             "ozaki_gemm: SYM_PAIRROW needs M == pair_n^2");
+  GB_REQUIRE(g.sym != SYM_PAIRCOL, GB_ERR_INVALID_ARG,
+             "ozaki_gemm: pair symmetry runs over the packed pair triangle here (SYM_TRIROW / SYM_TRICOL)");
   GB_REQUIRE(g.sym != SYM_TRIROW || (long long)g.pair_n * (g.pair_n + 1) / 2 == g.M, GB_ERR_BAD_SHAPE,
              "ozaki_gemm: SYM_TRIROW needs M == pair_n (pair_n + 1) / 2");
   GB_REQUIRE(g.sym != SYM_TRICOL || (long long)g.pair_n * (g.pair_n + 1) / 2 == g.N, GB_ERR_BAD_SHAPE,
@@ -1333,12 +1272,8 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   GB_TRY(configure_device());
   const KArgs ka = make_args(A, B, g);
   const long long tiles = ozaki_tiles(g);
-  // outputs whose tile rows are the unit stride take the persistent kernel;
-  // under pair symmetry (whole row bands skipped) only with the tile counter,
-  // as a static walk would desynchronise the CTAs that share a block of the
-  // large operand
-  const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1) &&
-                         ((g.sym != SYM_PAIRROW && g.sym != SYM_PAIRCOL) || g.tile_counter);
+  // outputs whose tile rows are the unit stride take the persistent kernel
+  const bool rows_fast = !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1);
   int dev = 0;
   cudaGetDevice(&dev);
   const int nsm = (dev >= 0 && dev < 64 && g_num_sms[dev] > 0) ? g_num_sms[dev] : 0;
