@@ -458,14 +458,19 @@ def jkj_ri_mixed(C: torch.Tensor, prep: PreparedRI, nbf5: int):
 
 
 _COPY_STREAMS: dict = {}
+_COPY_LOCK = threading.Lock()
 
 
-def _copy_stream(dev: torch.device) -> torch.cuda.Stream:
-    """A second stream per device for device-to-host copies."""
-    s = _COPY_STREAMS.get(dev)
-    if s is None:
-        s = _COPY_STREAMS[dev] = torch.cuda.Stream(device=dev)
-    return s
+def _copy_stream(dev: torch.device, main: torch.cuda.Stream) -> torch.cuda.Stream:
+    """A second stream for the device-to-host copies of work on ``main`` (one
+    per compute stream, so concurrent callers on their own streams never
+    wait on each other's copies)."""
+    key = (dev, main.cuda_stream)
+    with _COPY_LOCK:
+        s = _COPY_STREAMS.get(key)
+        if s is None:
+            s = _COPY_STREAMS[key] = torch.cuda.Stream(device=dev)
+        return s
 
 
 def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int = 2):
@@ -484,7 +489,8 @@ def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int =
     Jh = torch.empty((nbf5, N, N), dtype=_F64, pin_memory=True)
     Kh = torch.empty((nbf5, N, N), dtype=_F64, pin_memory=True)
     wp, wn = _ws("gb_jkj_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
-    main, cs = torch.cuda.current_stream(dev), _copy_stream(dev)
+    main = torch.cuda.current_stream(dev)
+    cs = _copy_stream(dev, main)
     _lib.call("gb_jkj_ri_mixed_j", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J), wp, wn, main.cuda_stream)
     cs.wait_stream(main)
     with torch.cuda.stream(cs):
