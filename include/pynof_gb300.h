@@ -228,6 +228,14 @@ int gb_rotate_orbital_f64(const double* y, const double* C, int nbf, int nbf5, d
 int gb_occ_energy_grad_f64(const double* gamma, const double* J_MO, const double* K_MO, const double* H_core,
                            int nbf5, int no1, int ndoc, int ncwo, double* energy, double* grad);
 
+/* A9  calce (pynof/pnof.py:905-929) on the HOST for given coefficients
+ * cj12, ck12 [nbf5][nbf5] (diagonals zeroed by the caller, as the reference
+ * does in place), occupations n and H_core [nbf5], J_MO, K_MO [nbf5][nbf5].
+ * Both this and gb_occ_energy_grad_f64 sum the energy with compensation
+ * (Neumaier). */
+int gb_calce_f64(const double* n, const double* cj12, const double* ck12, const double* J_MO, const double* K_MO,
+                 const double* H_core, int nbf5, int nbeta, int nalpha, double* energy);
+
 /* Plain FP64 GEMM C = A B^T with row-major A [M][K], B [N][K], C [M][N] on the
  * DMMA engine (the FP64 counterpart of gb_dgemm_mixed).  No counterpart in
  * the reference (numpy / cupy GEMMs); used e.g. for ERPA's (pq|sl) from b_pql

@@ -73,6 +73,7 @@ SIGNATURES = {
     "gb_rotate_orbital_workspace_f64": (_Z, [_I]),
     "gb_rotate_orbital_f64": (_I, [_P, _P, _I, _I, _c.c_double, _P, _P, _Z, _P]),
     "gb_occ_energy_grad_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "gb_calce_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
     "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
     "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),

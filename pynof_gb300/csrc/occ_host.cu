@@ -19,6 +19,8 @@
 //    also move with the pair's strong n_s.  So g = dn^T e, with e collected
 //    here per orbital (and per nd_i, then chained to n_i and n_s), with the
 //    1e-15 floors of the reference's denominators.
+// The energy is summed with compensation (its FP64 sums carry their rounding
+// errors), the occupation-space energy sums being kept in compensated FP64.
 // Closed shell without singly occupied orbitals (MSpin = 0, nsoc = 0).
 #include <cmath>
 #include <vector>
@@ -28,6 +30,22 @@
 namespace {
 
 constexpr double kHCut = 0.02 * 1.4142135623730951;  // H_CUT = 0.02 sqrt(2)
+
+// Neumaier's compensated summation (A. Neumaier, ZAMM 54 (1974) 39-51): the
+// rounding error of every addition is accumulated separately in c.
+struct CompSum {
+  double s = 0.0, c = 0.0;
+  void add(double x) {
+    const double t = s + x;
+    c += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  void add(const CompSum& o) {
+    add(o.s);
+    add(o.c);
+  }
+  double value() const { return s + c; }
+};
 
 struct OccLayout {
   int P, no1, ndoc, ncwo, nb;
@@ -89,18 +107,19 @@ extern "C" int gb_occ_energy_grad_f64(const double* gamma, const double* J, cons
   }
 
   // energy and dE/dn (e), dE/dnd (end_); pairs (a, b), a != b, of different pairs
-  double E = 0.0;
+  CompSum E;
   for (int i = 0; i < P; ++i) {
-    E += n[i] * (2.0 * H[i] + J[(size_t)i * P + i]);
+    E.add(n[i] * (2.0 * H[i] + J[(size_t)i * P + i]));
     e[i] = 2.0 * H[i] + J[(size_t)i * P + i];
   }
   for (int a = 0; a < P; ++a) {
     const int pa = pair_of[a];
-    double ea = 0.0, enda = 0.0, Ea = 0.0;
+    double ea = 0.0, enda = 0.0;
+    CompSum Ea;
     for (int b = 0; b < P; ++b) {
       if (b == a || (pa >= 0 && pair_of[b] == pa)) continue;
       const double Jba = J[(size_t)b * P + a], Kba = K[(size_t)b * P + a];
-      Ea += 2.0 * n[a] * n[b] * Jba;
+      Ea.add(2.0 * n[a] * n[b] * Jba);
       ea += 4.0 * n[b] * Jba;
       double ck = n[a] * n[b], dck = n[b];
       const bool chi = (cls[a] == 1 && cls[b] == 2) || (cls[a] == 2 && cls[b] >= 1);
@@ -110,10 +129,10 @@ extern "C" int gb_occ_energy_grad_f64(const double* gamma, const double* J, cons
         dck += fid[a] * fi[b];
         enda -= 2.0 * (sigma * nd12[b] / (2.0 * std::fmax(nd12[a], 1e-15)) - nd[b]) * Kba;
       }
-      Ea -= ck * Kba;
+      Ea.add(-ck * Kba);
       ea -= 2.0 * dck * Kba;
     }
-    E += Ea;
+    E.add(Ea);
     e[a] += ea;
     end_[a] += enda;
   }
@@ -126,19 +145,19 @@ extern "C" int gb_occ_energy_grad_f64(const double* gamma, const double* J, cons
       const int w = L.weak(p, j);
       const double Kws = K[(size_t)w * P + s], Ksw = K[(size_t)s * P + w];
       const double rw = std::sqrt(std::fmax(n[w], 1e-15));
-      E -= std::sqrt(n[s] * n[w]) * (Kws + Ksw);
+      E.add(-std::sqrt(n[s] * n[w]) * (Kws + Ksw));
       e[s] -= std::sqrt(n[w]) / rs * Kws;
       e[w] -= std::sqrt(n[s]) / rw * Ksw;
       for (int j2 = 0; j2 < ncwo; ++j2) {
         if (j2 == j) continue;
         const int w2 = L.weak(p, j2);
         const double Kw2w = K[(size_t)w2 * P + w];
-        E += std::sqrt(n[w] * n[w2]) * Kw2w;
+        E.add(std::sqrt(n[w] * n[w2]) * Kw2w);
         e[w] += std::sqrt(n[w2]) / rw * Kw2w;
       }
     }
   }
-  *energy = E;
+  *energy = E.value();
   if (!grad) return GB_OK;
   // nd_s = n_s F(n_s), nd_w = n_w F(n_s)
   for (int p = 0; p < ndoc; ++p) {
@@ -159,5 +178,29 @@ extern "C" int gb_occ_energy_grad_f64(const double* gamma, const double* J, cons
       grad[L.gam(p, j)] = -ns[p] * w * e[p] + w * e[L.weak(p, j)] - w * wsum;
     }
   }
+  return GB_OK;
+}
+
+// calce (pnof.py:905-929) for given coefficients: E = 2 sum_i n_i H_i
+// + sum_{i < nbeta} n_i J_ii + sum_{i >= nalpha} n_i J_ii
+// + sum_ij cj12_ij J_ji - sum_ij ck12_ij K_ji, with the compensated sum
+// (the caller zeroes the coefficients' diagonals, as the reference does).
+extern "C" int gb_calce_f64(const double* n, const double* cj12, const double* ck12, const double* J,
+                            const double* K, const double* H, int nbf5, int nbeta, int nalpha, double* energy) {
+  gb::clear_error();
+  GB_REQUIRE(n && cj12 && ck12 && J && K && H && energy, GB_ERR_INVALID_ARG, "gb_calce_f64: null pointer");
+  GB_REQUIRE(nbf5 >= 1 && 0 <= nbeta && nbeta <= nalpha && nalpha <= nbf5, GB_ERR_BAD_SHAPE,
+             "gb_calce_f64: need 0 <= nbeta <= nalpha <= nbf5 (%d, %d, %d)", nbeta, nalpha, nbf5);
+  const int P = nbf5;
+  CompSum E;
+  for (int i = 0; i < P; ++i) E.add(2.0 * n[i] * H[i]);
+  for (int i = 0; i < nbeta; ++i) E.add(n[i] * J[(size_t)i * P + i]);
+  for (int i = nalpha; i < P; ++i) E.add(n[i] * J[(size_t)i * P + i]);
+  for (int a = 0; a < P; ++a)
+    for (int b = 0; b < P; ++b) {
+      E.add(cj12[(size_t)a * P + b] * J[(size_t)b * P + a]);
+      E.add(-(ck12[(size_t)a * P + b] * K[(size_t)b * P + a]));
+    }
+  *energy = E.value();
   return GB_OK;
 }

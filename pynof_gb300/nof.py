@@ -177,13 +177,17 @@ def der_cjckd8(n, dn, p):
 
 def calce(n, cj12, ck12, J_MO, K_MO, H_core, p):
     """Closed-shell energy E(n) (``pnof.py:905-929``).  The diagonals of cj12 /
-    ck12 are zeroed in place, as in the reference."""
-    P = p.nbf5
+    ck12 are zeroed in place, as in the reference.  The terms are summed with
+    compensation (the library's ``gb_calce_f64``, host code): the
+    occupation-space energy sums are kept in compensated FP64."""
+    from . import _lib
+
     np.fill_diagonal(cj12, 0.0)
     np.fill_diagonal(ck12, 0.0)
-    dj = np.diagonal(J_MO)
-    E = 2.0 * np.dot(n, H_core) + np.dot(n[: p.nbeta], dj[: p.nbeta]) + np.dot(n[p.nalpha: P], dj[p.nalpha: P])
-    return E + np.sum(cj12 * J_MO.T) - np.sum(ck12 * K_MO.T)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (n, cj12, ck12, J_MO, K_MO, H_core)]
+    E = np.zeros(1)
+    _lib.call("gb_calce_f64", *(a.ctypes.data for a in args), p.nbf5, p.nbeta, p.nalpha, E.ctypes.data)
+    return float(E[0])
 
 
 # ---------------------------------------------------------------------------

@@ -77,3 +77,29 @@ def test_native_rejects_bad_layout():
     with pytest.raises(_lib.GBError):
         _lib.call("gb_occ_energy_grad_f64", np.zeros(8).ctypes.data, J.ctypes.data, J.ctypes.data,
                   np.zeros(4).ctypes.data, 4, 0, 2, 4, out.ctypes.data, None)
+
+
+def test_calce_sums_with_compensation():
+    """The energy sum keeps what plain FP64 summation loses: J_MO's large
+    entries cancel in pairs (J_ji = -J_ij at 2^40), so E is the sum of the
+    small dyadic parts alone (every product here is exact, so math.fsum of the
+    terms is the exact E)."""
+    import math
+    import types
+
+    P = 40
+    rng = np.random.default_rng(11)
+    i, j = np.indices((P, P))
+    big = np.triu(rng.choice([-1.0, 1.0], size=(P, P)), 1) * 2.0 ** 40 * ((i + j) % 2 == 0)
+    small = rng.integers(-2 ** 20, 2 ** 20, size=(P, P)) * 2.0 ** -40 * ((i + j) % 2 == 1)
+    J = big - big.T + small  # large entries on one checkerboard colour, small ones on the other
+    cj = np.ones((P, P))
+    ck = np.zeros((P, P))
+    p = types.SimpleNamespace(nbf5=P, nbeta=P // 2, nalpha=P // 2)
+    n = np.zeros(P)
+    E = nof.calce(n, cj.copy(), ck.copy(), J, np.zeros((P, P)), np.zeros(P), p)
+    np.fill_diagonal(cj, 0.0)
+    exact = math.fsum((cj * J.T).ravel())
+    plain = float(np.sum(cj * J.T))
+    print(f"exact {exact:.17g}  compensated {E:.17g}  plain {plain:.17g}")
+    assert abs(E - exact) < 1e-10
