@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default=WORKLOAD)
-    ap.add_argument("--cpu-sample", type=int, default=0, help="orbitals in the CPU sample (0 = auto)")
+    ap.add_argument("--cpu-reps", type=int, default=3, help="whole CPU-oracle builds timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
@@ -95,19 +95,21 @@ def n_products(S):
     return S * (S + 1) // 2
 
 
-def energy_from_jk(torch, J, K, C, H, n, cj, ck):
-    """Closed-shell electronic energy from J_i, K_i (FP64, torch):
+def energy_from_jk(J, K, C, H, n, cj, ck):
+    """Closed-shell electronic energy from J_i, K_i (FP64, numpy):
     E = sum_i C_i^T F_i C_i + sum_i n_i H_ii with the generalized Fock
     F_i = n_i H + n_i J_i + sum_j cj_ij J_j - sum_j ck_ij K_j (zero diagonals),
     i.e. computeF_RC -> computeLagrange -> computeE_elec with no1 = 0."""
     P = J.shape[0]
     Cp = C[:, :P]
-    Hd = torch.einsum("mi,mi->i", Cp, H @ Cp)
-    Jd = torch.einsum("mi,jmi->ji", Cp, torch.matmul(J, Cp))
-    Kd = torch.einsum("mi,jmi->ji", Cp, torch.matmul(K, Cp))
-    cj = cj.clone().fill_diagonal_(0.0)
-    ck = ck.clone().fill_diagonal_(0.0)
-    return float(2.0 * (n * Hd).sum() + (n * torch.diagonal(Jd)).sum() + (cj * Jd.T).sum() - (ck * Kd.T).sum())
+    Hd = np.einsum("mi,mi->i", Cp, H @ Cp)
+    Jd = np.einsum("mi,jmi->ji", Cp, np.matmul(J, Cp))
+    Kd = np.einsum("mi,jmi->ji", Cp, np.matmul(K, Cp))
+    cj = cj.copy()
+    ck = ck.copy()
+    np.fill_diagonal(cj, 0.0)
+    np.fill_diagonal(ck, 0.0)
+    return float(2.0 * np.dot(n, Hd) + np.dot(n, np.diagonal(Jd)) + np.sum(cj * Jd.T) - np.sum(ck * Kd.T))
 
 
 class ClockSampler:
@@ -171,22 +173,25 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(b, C, P, sample, N, Q):
-    """Oracle JKj_RI on the first `sample` orbitals, scaled to builds/s."""
+def cpu_baseline(b, C, P, N, Q, reps=3):
+    """The oracle's JKj_RI (numpy/OpenBLAS, every host thread) over all nbf5
+    orbitals: builds/s (median of ``reps`` whole builds) and the last build's
+    J, K, which the accuracy legs compare against."""
     from oracle import pynof_oracle as orc
 
     cores = os.cpu_count()
     orc.jkj_ri(C, b, 2)  # warm the BLAS threads
     times = []
-    for _ in range(5):
+    for _ in range(reps):
         t0 = time.perf_counter()
-        orc.jkj_ri(C, b, sample)
+        J, K = orc.jkj_ri(C, b, P)
         times.append(time.perf_counter() - t0)
     t = statistics.median(times)
-    return {"value": (sample / P) / t, "unit": "builds/s", "cores": cores, "kind": "port",
-            "sample": f"J_i, K_i for {sample} of {P} orbitals at nbf={N}, naux={Q} (median of 5; scaled by "
-                      f"{sample}/{P}; numpy/OpenBLAS restatement of JKj_RI)",
-            "seconds_per_sample": t}
+    rec = {"value": 1.0 / t, "unit": "builds/s", "cores": cores, "kind": "port",
+           "sample": f"whole builds (J_i, K_i for all {P} orbitals) at nbf={N}, naux={Q}, median of {reps}; "
+                     "numpy/OpenBLAS restatement of JKj_RI",
+           "seconds_per_build": t}
+    return rec, J, K
 
 
 def make_workload(name):
@@ -205,22 +210,22 @@ def run_reference(args):
     N, P, Q = st.nbf, st.nbf5, st.nbfaux
     from oracle import pynof_oracle as orc
 
-    sample = args.cpu_sample or max(2, P // 5)
     orc.jkj_ri(C, b, 2)
     for _ in range(args.warmup):
-        orc.jkj_ri(C, b, sample)
+        orc.jkj_ri(C, b, P)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        orc.jkj_ri(C, b, sample)
+        orc.jkj_ri(C, b, P)
     dt = time.perf_counter() - t0
-    value = args.steps * (sample / P) / dt
+    value = args.steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P}", "sample_orbitals": sample},
+        "config": {"workload": f"RI JK build nbf={N} naux={Q} nbf5={P} (computeJKj)"},
         "cpu_baseline": {"value": value, "unit": "builds/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"J_i, K_i for {sample} of {P} orbitals per step, scaled by {sample}/{P}"},
+                         "sample": f"one whole build (J_i, K_i for all {P} orbitals) per step; numpy/OpenBLAS "
+                                   "restatement of JKj_RI on every host thread"},
         "e2e": {"value": value, "unit": "builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -309,8 +314,42 @@ def run_ours(args):
     d2h = 2 * P * N * N * 8
     del Jh, Kh
 
-    # ---- FP64 DMMA comparison leg and accuracy of the headline path ------
+    # ---- computeJKH_MO and computeLagrange2 (what the solve loop calls) ---
+    from pynof_gb300 import nof
+
+    dH = ops.to_device(H)
+    dn = ops.to_device(n)
+    cj_h, ck_h = nof.cjckd8(n, st)
+    np.fill_diagonal(cj_h, 0.0)
+    np.fill_diagonal(ck_h, 0.0)
+    dcj, dck = ops.to_device(cj_h), ops.to_device(ck_h)
+
+    def timed(fn, count):
+        fn()
+        barrier()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(count):
+            fn()
+        t1.record(stream)
+        barrier()
+        return count * world / reps.max(t0.elapsed_time(t1) / 1e3)
+
+    rates = {"unit": "calls/s", "jkh_mo_per_s": {}, "lagrange2_per_s": {}}
+    if mixed:
+        rates["jkh_mo_per_s"]["mixed"] = timed(lambda: ops.jkh_mo_ri_mixed(dC, dH, prep, P), args.steps)
+        rates["lagrange2_per_s"]["mixed"] = timed(
+            lambda: ops.lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta, st.nalpha), args.steps)
+        ops.check_device_status()
+    if args.fp64_steps > 0 or not mixed:
+        k64 = max(1, args.fp64_steps)
+        rates["jkh_mo_per_s"]["fp64"] = timed(lambda: ops.jkh_mo_ri(dC, dH, db, P), k64)
+        rates["lagrange2_per_s"]["fp64"] = timed(
+            lambda: ops.lagrange2_ri(dC, dH, db, dn, dcj, dck, P, st.nbeta, st.nalpha), k64)
+
+    # ---- FP64 DMMA comparison leg -----------------------------------------
     fp64 = None
+    J64h = K64h = None
     if mixed and args.fp64_steps > 0:
         J64, K64 = ops.jkj_ri(dC, db, P)
         barrier()
@@ -321,23 +360,47 @@ def run_ours(args):
         f1.record(stream)
         barrier()
         fp64_s = reps.max(f0.elapsed_time(f1) / 1e3)
-        dH = ops.to_device(H)
-        dn = ops.to_device(n)
-        cj = 2.0 * torch.outer(dn, dn)
-        ck = torch.outer(dn, dn)
-        E64 = energy_from_jk(torch, J64, K64, dC, dH, dn, cj, ck)
-        Emx = energy_from_jk(torch, J, K, dC, dH, dn, cj, ck)
-
-        def nrel(a, r):
-            return float((a - r).abs().max() / r.abs().max())
-
         fp64 = {"value": world * args.fp64_steps / fp64_s, "unit": "builds/s", "steps": args.fp64_steps,
                 "ms_per_step": 1e3 * fp64_s / args.fp64_steps,
-                "speedup_of_headline": value / (world * args.fp64_steps / fp64_s),
-                "J_normwise_err": nrel(J, J64), "K_normwise_err": nrel(K, K64),
-                "E_fp64_hartree": E64, "E_abs_err_hartree": abs(Emx - E64),
-                "energy_note": "closed-shell E from J_i, K_i with cj=2nn^T, ck=nn^T (zero diagonals)"}
+                "speedup_of_headline": value / (world * args.fp64_steps / fp64_s)}
+        J64h, K64h = J64.cpu().numpy(), K64.cpu().numpy()
         del J64, K64
+    Jh, Kh = J.cpu().numpy(), K.cpu().numpy()
+    del J, K
+    torch.cuda.empty_cache()
+
+    # ---- CPU oracle: baseline rate and the accuracy of both device paths ---
+    cpu = accuracy = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import pynof_oracle as orc
+
+        cpu, Jr, Kr = cpu_baseline(b, C, P, N, Q, reps=args.cpu_reps)
+        t0 = time.perf_counter()
+        orc.jkh_mo_ri(C, H, b, P)
+        cpu["jkh_mo_per_s"] = 1.0 / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        orc.lagrange2(n, cj_h.copy(), ck_h.copy(), C, H, None, b, st)
+        cpu["lagrange2_per_s"] = 1.0 / (time.perf_counter() - t0)
+        rates["jkh_mo_per_s"]["cpu_oracle"] = cpu["jkh_mo_per_s"]
+        rates["lagrange2_per_s"]["cpu_oracle"] = cpu["lagrange2_per_s"]
+
+        def nrel(a, r):
+            return float(np.max(np.abs(a - r)) / np.max(np.abs(r)))
+
+        E_ref = energy_from_jk(Jr, Kr, C, H, n, cj_h, ck_h)
+        accuracy = {"reference": "the CPU oracle (numpy FP64 restatement of JKj_RI) on the same inputs",
+                    "energy_definition": "closed-shell E from J_i, K_i: computeF_RC -> computeLagrange -> "
+                                         "computeE_elec with GNOF cj12, ck12 (zero diagonals), no1 = 0",
+                    "E_oracle_hartree": E_ref, "headline": {
+                        "J_normwise_err": nrel(Jh, Jr), "K_normwise_err": nrel(Kh, Kr),
+                        "E_abs_err_hartree": abs(energy_from_jk(Jh, Kh, C, H, n, cj_h, ck_h) - E_ref)}}
+        if J64h is not None:
+            accuracy["fp64_dmma"] = {"J_normwise_err": nrel(J64h, Jr), "K_normwise_err": nrel(K64h, Kr),
+                                     "E_abs_err_hartree": abs(energy_from_jk(J64h, K64h, C, H, n, cj_h, ck_h) -
+                                                              E_ref)}
+        del Jr, Kr
+    if fp64 is not None and accuracy is not None:
+        fp64["E_abs_err_hartree_vs_oracle"] = accuracy["fp64_dmma"]["E_abs_err_hartree"]
 
     # ---- roofline of the dominant kernel ---------------------------------
     peaks, peak_src = measured_peaks()
@@ -391,10 +454,11 @@ def run_ours(args):
         "gpu_launches": sum(v[0] for v in prof.values()),
         "clocks": clk,
         "fp64_path": fp64,
+        "hot_path_rates": rates,
+        "accuracy": accuracy,
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        sample = args.cpu_sample or max(2, P // 5)
-        line["cpu_baseline"] = cpu_baseline(b, C, P, sample, N, Q)
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
     reps.close()

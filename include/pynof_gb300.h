@@ -80,8 +80,9 @@ int gb_jkj_ri_f64(const double* C, const double* b, int nbf, int nbf5, int naux,
  * loads this library until the process exits; problems whose workspace
  * (gb_jkj_ri_workspace_f64) exceeds it are rejected with GB_ERR_WORKSPACE.
  * The first call on a device looks the array's address up (make it before any
- * stream capture).  All calls share the array: calls that overlap on the GPU
- * race and must be serialised on one stream. */
+ * stream capture; after a cudaDeviceReset the next call looks it up again).
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised on one stream. */
 #define GB_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int gb_jkj_ri_noalloc_f64(const double* C, const double* b, int nbf, int nbf5, int naux, double* J, double* K,
                           void* stream);
@@ -187,6 +188,22 @@ int gb_fock_rc_f64(const double* J, const double* K, const double* n, const doub
                    const double* ck12, int nbf, int nbf5, int nbeta, int nalpha, int no1, double* F, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* A8  computeF_RO (restricted open shell).  Replaces computeF_RO_GPU
+ *     (pynof/utils.py:172-246), reached from ENERGY1r when no1 > 0 and
+ *     MSpin != 0 (pynof/utils.py:423-425).  Same arguments as
+ *     gb_fock_rc_f64; with D = [0, nbeta) u [nalpha, nbf5) and the singly
+ *     occupied O = [nbeta, nalpha):
+ *     F_i = a_i H + sum_j A_ij J_j - sum_j B_ij K_j,  a_i = n_i (D), 1/2 (O);
+ *     A_ij = cj12_ij (i, j in D) + n_i [i == j, ini <= i < nbeta or i >= nalpha]
+ *          + n_i (i in D, j in O) + 1/2 (i != j in O) + n_j (i in O, j in D);
+ *     B_ij = ck12_ij (i, j in D) + n_i / 2 (i in D, j in O) + 1/2 (i != j in O)
+ *          + n_j / 2 (i in O, j in D); the diagonal entries (i, i), i >= ini,
+ *     of cj12 / ck12 ignored. */
+size_t gb_fock_ro_workspace_f64(int nbf, int nbf5);
+int gb_fock_ro_f64(const double* J, const double* K, const double* n, const double* H, const double* cj12,
+                   const double* ck12, int nbf, int nbf5, int nbeta, int nalpha, int no1, double* F, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* A8  computeLagrange (pynof/utils.py:249-259):
  *     elag[k][i] = sum_mn C[m][k] F_i[m][n] C[n][i] for k < noptorb, i < nbf5; 0 elsewhere. */
 size_t gb_lagrange_workspace_f64(int nbf, int nbf5);
@@ -271,10 +288,27 @@ int gb_graph_destroy(gb_graph* graph);
 
 #define GB_SPLIT_TF32X3 32
 
-/* Status word of the tensor-core kernels on the current device: 0, or
- * GB_ERR_TIMEOUT when one of their bounded waits gave up.  Synchronises the
- * device; reset != 0 clears the word. */
+/* Status word of the tensor-core kernels on the current device: 0, or the
+ * first error one of them recorded -- GB_ERR_TIMEOUT when a bounded wait gave
+ * up, GB_ERR_NONFINITE when an operand held a NaN or an infinity (digit
+ * slices cannot represent it).  Once set, every later split-product GEMM
+ * launch on the device returns without work until the word is cleared
+ * (reset != 0), so every caller that reads it after its own work sees the
+ * failure.  Synchronises the device.  No counterpart in the reference, which
+ * has no device-side failure reporting. */
 int gb_device_status(int reset, int* status);
+
+/* Limit of every bounded wait inside the split-product kernels launched after
+ * this call, in nanoseconds (0 restores the default of 2 s).  No counterpart
+ * in the reference. */
+int gb_set_wait_limit_ns(unsigned long long limit_ns);
+
+/* Test hook for the timeout path, no counterpart in the reference: while
+ * stage >= 0, the first CTA of every split-product GEMM launched afterwards
+ * never issues the copy of that pipeline stage, so its wait for the stage
+ * runs out (after the wait limit), the kernel gives up cleanly and
+ * GB_ERR_TIMEOUT is recorded.  stage < 0 turns it off. */
+int gb_test_withhold_stage(int stage);
 
 /* Generic FP64-accurate GEMM on the tensor cores: C = A B^T with row-major
  * A [M][K], B [N][K], C [M][N].  No counterpart in the reference (PyNOF's

@@ -184,6 +184,41 @@ def fock_rc(J, K, n, H, cj12, ck12, p):
     return F
 
 
+def fock_ro(J, K, n, H, cj12, ck12, p):
+    """F_i (P, N, N) restricted open shell (``utils.py:97-169`` computeF_RO_CPU).
+
+    Index blocks: D = [0, nbeta) and [nalpha, P) (doubly occupied and
+    correlating orbitals), O = [nbeta, nalpha) (singly occupied).  Step by step
+    as the reference: n_i H on D and H / 2 on O; n_i J_i on [ini, nbeta) and
+    [nalpha, P); the C^J J and -C^K K couplings inside D (diagonals from ini
+    on zeroed in place); the D-O terms n_i sum_{j in O} (J_j - K_j / 2); for O,
+    (1/2) sum_{j in O, j != i} (J_j - K_j) plus sum_{j in D} n_j (J_j - K_j / 2).
+    """
+    P, nb, na = p.nbf5, p.nbeta, p.nalpha
+    ini = p.no1 if p.no1 > 1 else 0
+    N = J.shape[1]
+    D = np.r_[0:nb, na:P]
+    O = np.arange(nb, na)
+    F = np.zeros((P, N, N))
+    F[D] += n[D, None, None] * H[None]
+    F[O] += 0.5 * H[None]
+    F[ini:nb] += n[ini:nb, None, None] * J[ini:nb]
+    F[na:P] += n[na:P, None, None] * J[na:P]
+    _zero_diag(cj12[ini:, ini:])
+    _zero_diag(ck12[ini:, ini:])
+    JD = J[D].reshape(len(D), N * N)
+    KD = K[D].reshape(len(D), N * N)
+    F[D] += (cj12[np.ix_(D, D)] @ JD - ck12[np.ix_(D, D)] @ KD).reshape(len(D), N, N)
+    if len(O):
+        WO = (J[O] - 0.5 * K[O]).sum(axis=0)                       # sum_{j in O} (J_j - K_j / 2)
+        F[D] += n[D, None, None] * WO[None]
+        VO = (J[O] - K[O]).sum(axis=0)
+        F[O] += 0.5 * VO[None] - 0.5 * (J[O] - K[O])               # j != i within O
+        WD = np.tensordot(n[D], J[D] - 0.5 * K[D], axes=1)         # sum_{j in D} n_j (J_j - K_j / 2)
+        F[O] += WD[None]
+    return F
+
+
 def lagrange(F, C, p):
     """elag from F (``utils.py:249-259`` computeLagrange)."""
     P, N, no = p.nbf5, p.nbf, p.noptorb
@@ -214,14 +249,14 @@ def lagrange_convergency(elag):
 
 
 def energy1r(C, n, H, I, b, cj12, ck12, p):
-    """E, elag, sumdiff, maxdiff (``utils.py:414-431`` ENERGY1r); closed shell."""
+    """E, elag, sumdiff, maxdiff (``utils.py:414-431`` ENERGY1r)."""
     P = p.nbf5
     if p.no1 == 0:
         elag, Hmat = lagrange2(n, cj12, ck12, C, H, I, b, p)
         E = np.trace(elag[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat)[:P])
     else:
         J, K = jkj_ri(C, b, P) if p.RI else jkj_full(C, I, P)
-        F = fock_rc(J, K, n, H, cj12, ck12, p)
+        F = fock_rc(J, K, n, H, cj12, ck12, p) if p.MSpin == 0 else fock_ro(J, K, n, H, cj12, ck12, p)
         elag = lagrange(F, C, p)
         E = e_elec(H, C, n, elag, p)
     s, m = lagrange_convergency(elag)

@@ -55,6 +55,8 @@ SIGNATURES = {
     "gb_lagrange2_full_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
     "gb_fock_rc_workspace_f64": (_Z, [_I, _I]),
     "gb_fock_rc_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_fock_ro_workspace_f64": (_Z, [_I, _I]),
+    "gb_fock_ro_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_lagrange_workspace_f64": (_Z, [_I, _I]),
     "gb_lagrange_f64": (_I, [_P, _P, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_energy_elec_workspace_f64": (_Z, [_I, _I]),
@@ -75,6 +77,8 @@ SIGNATURES = {
     "gb_occ_energy_grad_f64": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _P, _P]),
     "gb_calce_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),
+    "gb_set_wait_limit_ns": (_I, [_c.c_ulonglong]),
+    "gb_test_withhold_stage": (_I, [_I]),
     "gb_dgemm_mixed_workspace": (_Z, [_I, _I, _I, _I]),
     "gb_dgemm_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_ri_prepare_bytes_mixed": (_Z, [_I, _I, _I]),

@@ -70,8 +70,17 @@ class BatchJK:
         """Replay the graph on the plan's stream (asynchronous)."""
         _lib.call("gb_batch_launch", self.plan, self.stream.cuda_stream)
 
+    def wait(self):
+        """Wait for the replays issued so far; raise GBError if a kernel of
+        the batch recorded a timeout or met a non-finite operand."""
+        self.stream.synchronize()
+        ops.check_device_status()
+
     def close(self):
+        """Destroy the graph once every replay has finished: the outputs and
+        the workspace go back to torch's allocator only after that."""
         if self.plan:
+            self.stream.synchronize()
             _lib.call("gb_batch_destroy", self.plan)
             self.plan = None
 

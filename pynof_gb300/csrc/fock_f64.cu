@@ -1,5 +1,5 @@
 // Generalized Fock matrices, the Lagrangian from them and the electronic
-// energy (FP64): computeF_RC, computeLagrange, computeE_elec.
+// energy (FP64): computeF_RC, computeF_RO, computeLagrange, computeE_elec.
 #include "gemm_f64.cuh"
 #include "ri_kernels.cuh"
 
@@ -29,6 +29,56 @@ __global__ void fock_diag_terms_kernel(double* __restrict__ F, const double* __r
   double v = F[o] + ni * H[mn];
   if (cj) v += ni * J[o];
   F[o] = v;
+}
+
+// Coupling coefficients of the restricted open-shell generalized Fock
+//   F_i = a_i H + sum_j A[i][j] J_j - sum_j B[i][j] K_j
+// with D = [0, nbeta) u [nalpha, P) (doubly occupied and correlating) and
+// O = [nbeta, nalpha) (singly occupied):
+//   a_i = n_i on D, 1/2 on O;
+//   A[i][j] = cj12[i][j] (i, j in D; diagonal from ini on zero)
+//           + n_i (i == j, i in [ini, nbeta) or [nalpha, P))
+//           + n_i (i in D, j in O) + 1/2 (i, j in O, i != j) + n_j (i in O, j in D)
+//   B[i][j] = ck12[i][j] (i, j in D; diagonal from ini on zero)
+//           + n_i / 2 (i in D, j in O) + 1/2 (i, j in O, i != j) + n_j / 2 (i in O, j in D)
+// One thread per (i, j); the (i, 0) threads also write a_i.
+__global__ void fock_ro_coef_kernel(const double* __restrict__ n, const double* __restrict__ cj12,
+                                    const double* __restrict__ ck12, double* __restrict__ A, double* __restrict__ B,
+                                    double* __restrict__ a, int P, int ini, int nbeta, int nalpha) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)P * P) return;
+  const int i = (int)(idx / P), j = (int)(idx % P);
+  const bool oi = i >= nbeta && i < nalpha, oj = j >= nbeta && j < nalpha;
+  double av = 0.0, bv = 0.0;
+  if (!oi && !oj) {
+    const bool zero = (i == j && i >= ini);
+    av = zero ? 0.0 : cj12[idx];
+    bv = zero ? 0.0 : ck12[idx];
+    if (i == j && ((i >= ini && i < nbeta) || i >= nalpha)) av += n[i];
+  } else if (!oi && oj) {
+    av = n[i];
+    bv = 0.5 * n[i];
+  } else if (oi && oj) {
+    av = i != j ? 0.5 : 0.0;
+    bv = av;
+  } else {
+    av = n[j];
+    bv = 0.5 * n[j];
+  }
+  A[idx] = av;
+  B[idx] = bv;
+  if (j == 0) a[i] = oi ? 0.5 : n[i];
+}
+
+// F[i] += a_i H
+__global__ void fock_add_h_kernel(double* __restrict__ F, const double* __restrict__ H, const double* __restrict__ a,
+                                  int N) {
+  const long long mn = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  const long long NN = (long long)N * N;
+  if (mn >= NN) return;
+  const long long o = (long long)i * NN + mn;
+  F[o] = fma(a[i], H[mn], F[o]);
 }
 
 // G[i][m] = sum_n F[i][m][n] C[n][i]   (one warp per (i, m))
@@ -127,6 +177,56 @@ extern "C" int gb_fock_rc_f64(const double* J, const double* K, const double* n,
   GB_TRY(gemm_f64(g, s));
   GB_LAUNCH("fock_diag_terms", s,
             fock_diag_terms_kernel<<<dim3(cdiv(NN, 256), P), 256, 0, s>>>(F, J, H, n, N, P, ini, nbeta, nalpha));
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// A8  computeF_RO (restricted open shell)
+// ---------------------------------------------------------------------------
+extern "C" size_t gb_fock_ro_workspace_f64(int nbf, int nbf5) {
+  Sizer z;
+  z.add<double>((size_t)nbf5 * nbf5);
+  z.add<double>((size_t)nbf5 * nbf5);
+  z.add<double>((size_t)nbf5);
+  (void)nbf;
+  return z.used;
+}
+
+extern "C" int gb_fock_ro_f64(const double* J, const double* K, const double* n, const double* H,
+                              const double* cj12, const double* ck12, int nbf, int nbf5, int nbeta, int nalpha,
+                              int no1, double* F, void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5;
+  GB_REQUIRE(N > 0 && P > 0 && P <= N, GB_ERR_BAD_SHAPE, "gb_fock_ro_f64: bad sizes nbf=%d nbf5=%d", N, P);
+  GB_REQUIRE(0 <= nbeta && nbeta <= nalpha && nalpha <= P && no1 >= 0 && no1 <= nbeta, GB_ERR_BAD_SHAPE,
+             "gb_fock_ro_f64: need 0 <= no1 <= nbeta <= nalpha <= nbf5");
+  GB_REQUIRE(J && K && n && H && cj12 && ck12 && F, GB_ERR_INVALID_ARG, "gb_fock_ro_f64: null pointer");
+  Carve cv(workspace, workspace_bytes);
+  double* A = cv.take<double>((size_t)P * P);
+  double* B = cv.take<double>((size_t)P * P);
+  double* a = cv.take<double>((size_t)P);
+  GB_REQUIRE(A && B && a, GB_ERR_WORKSPACE, "gb_fock_ro_f64: workspace too small");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int ini = no1 > 1 ? no1 : 0;
+  GB_LAUNCH("fock_ro_coef", s,
+            fock_ro_coef_kernel<<<cdiv((long long)P * P, 256), 256, 0, s>>>(n, cj12, ck12, A, B, a, P, ini, nbeta,
+                                                                             nalpha));
+  const long long NN = (long long)N * N;
+  // F = A J - B K
+  GemmF64 g{};
+  g.M = P; g.N = (int)NN; g.K = P; g.batch = 1;
+  g.A = {A, 0, lin(P), lin(1)};
+  g.B = {J, 0, lin(NN), lin(1)};
+  g.C = {F, 0, lin(NN), lin(1)};
+  g.alpha = 1.0; g.beta = 0.0; g.sym = SYM_NONE;
+  g.a_kfast = true; g.b_kfast = false;
+  g.tag = "gemm_f64:fock";
+  GB_TRY(gemm_f64(g, s));
+  g.A = {B, 0, lin(P), lin(1)};
+  g.B = {K, 0, lin(NN), lin(1)};
+  g.alpha = -1.0; g.beta = 1.0;
+  GB_TRY(gemm_f64(g, s));
+  GB_LAUNCH("fock_add_h", s, fock_add_h_kernel<<<dim3(cdiv(NN, 256), P), 256, 0, s>>>(F, H, a, N));
   return GB_OK;
 }
 

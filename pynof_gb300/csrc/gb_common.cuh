@@ -20,6 +20,16 @@ void clear_error();
 int prof_begin(const char* name, cudaStream_t s);
 void prof_end(int idx, cudaStream_t s);
 
+// Id of the calling thread's current CUDA context (cuCtxGetId; unique for the
+// life of the process, so a context re-created after cudaDeviceReset gets a
+// new one), 0 when there is none.
+unsigned long long current_context_id();
+
+// Device address of the tensor-core status word (GB_OK, or the first
+// GB_ERR_TIMEOUT / GB_ERR_NONFINITE a kernel recorded) on the current device;
+// nullptr if it cannot be looked up.  Looked up once per device context.
+int* device_status_word();
+
 // Round up to a multiple of 256 bytes (every workspace carve is 256-aligned).
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 

@@ -12,11 +12,15 @@
 // driver reserves it on every GPU where this library's module is loaded and it
 // stays reserved until the process exits.  Host code cannot use the array's
 // name as a device address (on the host it names a host-side stand-in), so the
-// device address is looked up once per device with cudaGetSymbolAddress, with
-// that device current, and passed to the kernels as a plain pointer.
+// device address is looked up with cudaGetSymbolAddress, with the device
+// current, and passed to the kernels as a plain pointer.  The address is
+// cached per device together with the id of the context it belongs to; a
+// context created anew (after cudaDeviceReset) has a new id and the next call
+// looks the address up again.
 //
-// The first call on each device performs that lookup (which may also load the
-// module on that device); make that first call before any stream capture.
+// The first call on each device (and the first after a cudaDeviceReset)
+// performs that lookup, which may also load the module on that device; make
+// that call before any stream capture.
 //
 // Every call on a device uses the same array, and the array keeps whatever the
 // previous call left in it.  No part of it needs clearing: every scratch
@@ -35,20 +39,24 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // context id the cached address belongs to
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device context).
 int scratch_address(void** out) {
   int dev = -1;
   GB_TRY(gb::cuda_status(cudaGetDevice(&dev), "gb_jkj_ri_noalloc_f64: cudaGetDevice"));
   GB_REQUIRE(dev >= 0 && dev < kMaxDevices, GB_ERR_UNSUPPORTED,
              "gb_jkj_ri_noalloc_f64: device ordinal %d beyond %d", dev, kMaxDevices);
+  const unsigned long long ctx = gb::current_context_id();
   std::lock_guard<std::mutex> lk(g_mu);
-  if (g_scratch_addr[dev] == nullptr) {
+  if (g_scratch_addr[dev] == nullptr || ctx == 0 || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
     GB_TRY(gb::cuda_status(cudaGetSymbolAddress(&p, g_noalloc_scratch),
                            "gb_jkj_ri_noalloc_f64: cudaGetSymbolAddress"));
     GB_REQUIRE(p != nullptr, GB_ERR_CUDA, "gb_jkj_ri_noalloc_f64: null scratch address");
     g_scratch_addr[dev] = p;
+    g_scratch_ctx[dev] = gb::current_context_id();
   }
   *out = g_scratch_addr[dev];
   return GB_OK;

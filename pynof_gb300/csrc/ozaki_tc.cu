@@ -17,11 +17,15 @@
 // One launch covers one GEMM (optionally batched), or -- the grouped kernel --
 // a table of GEMMs of different shapes (e.g. one per molecule of a batch).
 //
-// Every mbarrier wait is bounded (kWaitLimitNs); on timeout the CTA records
-// GB_ERR_TIMEOUT in the device status word, stops issuing work, waits (bounded)
-// for its own TMA copies and MMAs in flight, frees TMEM and exits.
+// Every mbarrier wait is bounded (the launch's wait_ns, 2 s unless
+// gb_set_wait_limit_ns changed it); on timeout the CTA records GB_ERR_TIMEOUT
+// in the device status word, stops issuing work, waits (bounded) for its own
+// TMA copies and MMAs in flight, frees TMEM and exits.
 #include <cuda_bf16.h>
 
+#include <cuda.h>
+
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -58,7 +62,6 @@ struct TileCfg {
 };
 // bytes of the per-tile assembly tables (see cta_tile)
 __host__ __device__ constexpr uint32_t epi_table_bytes(int BN) { return 20u * (uint32_t)(BM + BN); }
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
 constexpr float MAGIC = 12582912.0f;                          // 1.5 * 2^23
 constexpr int MAGIC_BITS = 0x4B400000;
 
@@ -94,15 +97,15 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait.  Returns false on timeout, or (if abort_flag != nullptr) as soon
+// Bounded wait: false after limit_ns, or (if abort_flag != nullptr) as soon
 // as another role has aborted.
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try(bar, parity)) return true;
     if (abort_flag && *abort_flag) return false;
-    if ((it & 63) == 0 && now_ns() - t0 > kWaitLimitNs) return false;
+    if ((it & 63) == 0 && now_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -119,9 +122,11 @@ __device__ __forceinline__ bool epi_barrier_any(bool pred) {
   return r != 0;
 }
 
+// The first error recorded in the status word stays (a timeout does not
+// overwrite an earlier non-finite report, nor the other way round).
 __device__ __forceinline__ void signal_abort(volatile int* abort_flag) {
   *abort_flag = 1;
-  atomicExch(&g_tc_status, GB_ERR_TIMEOUT);
+  atomicCAS(&g_tc_status, 0, GB_ERR_TIMEOUT);
 }
 
 // Contiguous global -> shared bulk copy completing on an mbarrier.
@@ -234,6 +239,10 @@ struct KArgs {
   OzGemm g;
   SlicedDesc A, B;
   int frac;
+  unsigned long long wait_ns;  // limit of every mbarrier wait
+  // Test hook: the first CTA's producer never issues global stage `withhold`
+  // (-1: every stage is issued), so the MMA issuer's wait for it runs out.
+  int withhold;
 };
 
 // MMAs of one stage, fully unrolled for S slices: a product (s, t) reads slice
@@ -370,10 +379,10 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   const int n_mma = (n_valid + 15) & ~15;
   const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
 
+  int issued = 0;  // stages the producer handled (its lane 0)
   if (warp == 0) {
     // ---------------- producer ----------------
     if (lane == 0) {
-      int issued = 0;
       // an operand sliced once (batch 1) is shared by every batch entry
       const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
       const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
@@ -384,9 +393,13 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       for (int kb = 0; kb < nkb; ++kb) {
         const int st = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
-        if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag)) {
+        if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag, a.wait_ns)) {
           signal_abort(abort_flag);
           break;
+        }
+        if (kb == a.withhold && blockIdx.x == 0 && blockIdx.y == 0) {
+          ++issued;  // test hook: this stage never arrives
+          continue;
         }
         mbar_expect_tx(full_bar(st), stage_bytes);
         const uint32_t sa = sbase + st * stage_bytes;
@@ -405,11 +418,6 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         }
         ++issued;
       }
-      if (*abort_flag) {
-        // let the copies this thread issued land before the CTA exits
-        for (int kb = max(0, issued - STAGES); kb < issued; ++kb)
-          mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1, nullptr);
-      }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -417,7 +425,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       bool f_started = false;
       for (int kb = 0; kb < nkb; ++kb) {
         const int st = kb % STAGES;
-        if (!mbar_wait(full_bar(st), (kb / STAGES) & 1, abort_flag)) {
+        if (!mbar_wait(full_bar(st), (kb / STAGES) & 1, abort_flag, a.wait_ns)) {
           signal_abort(abort_flag);
           break;
         }
@@ -430,7 +438,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
           const int c = kb / CH, bsel = c & 1;
           if ((kb % CH) == 0) {
             if (c >= 2) {
-              if (!mbar_wait(bsel ? accempty1_bar : accempty_bar, ((c >> 1) - 1) & 1, abort_flag)) {
+              if (!mbar_wait(bsel ? accempty1_bar : accempty_bar, ((c >> 1) - 1) & 1, abort_flag, a.wait_ns)) {
                 signal_abort(abort_flag);
                 break;
               }
@@ -448,7 +456,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         if (g.fdrain) {
           // the FP32 accumulator is drained with the exact groups: restart it every chunk
           if (first && c > 0) {
-            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
+            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
               signal_abort(abort_flag);
               break;
             }
@@ -459,7 +467,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         } else {
           if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
           if (first && c > 0) {
-            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag)) {
+            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
               signal_abort(abort_flag);
               break;
             }
@@ -527,7 +535,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         // R (units of 2^-31) += rint(F 2^31): |F| < 2^7 per chunk of 96 k
         // (every |tf32 operand| < 1), so F 2^15 < 2^22 suits split_round
         const int bsel = c & 1;
-        const bool got = mbar_wait(bsel ? accfull1_bar : accfull_bar, (c >> 1) & 1, abort_flag);
+        const bool got = mbar_wait(bsel ? accfull1_bar : accfull_bar, (c >> 1) & 1, abort_flag, a.wait_ns);
         if (!__all_sync(0xffffffffu, got)) {
           signal_abort(abort_flag);
           ok = false;
@@ -549,7 +557,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         if (lane == 0) mbar_arrive(bsel ? accempty1_bar : accempty_bar);
         continue;
       }
-      const bool got = mbar_wait(accfull_bar, c & 1, abort_flag);
+      const bool got = mbar_wait(accfull_bar, c & 1, abort_flag, a.wait_ns);
       if (!__all_sync(0xffffffffu, got)) {
         signal_abort(abort_flag);
         ok = false;
@@ -597,7 +605,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       if (lane == 0) mbar_arrive(accempty_bar);
     }
     if (ok) {
-      const bool got = mbar_wait(done_bar, 0, abort_flag);
+      const bool got = mbar_wait(done_bar, 0, abort_flag, a.wait_ns);
       if (!__all_sync(0xffffffffu, got)) signal_abort(abort_flag);
     }
     // CTA-uniform go / no-go for the assembly (every epilogue warp arrives here)
@@ -701,10 +709,16 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
   }
 
   __syncthreads();
+  // the abort flag is final here: after an abort, the copies the producer
+  // issued must land before the CTA exits (a withheld stage's wait runs out)
+  if (warp == 0 && lane == 0 && *abort_flag) {
+    for (int kb = max(0, issued - STAGES); kb < issued; ++kb)
+      mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1, nullptr, a.wait_ns);
+  }
   if (warp == 1) {
     if (*abort_flag) {
       // every MMA this CTA issued must be complete before TMEM is released
-      mbar_wait(done_bar, 0, nullptr);
+      mbar_wait(done_bar, 0, nullptr, a.wait_ns);
     }
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::TMEM_COLS) : "memory");
@@ -790,15 +804,16 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   const int nkb = (g.K + BK - 1) / BK;
   const int nchunks = (nkb + CH - 1) / CH;
 
+  int gkb_issued = 0;  // stages the producer handled, all tiles (its lane 0)
   if (warp == 0) {
     // ---------------- producer ----------------
     if (lane == 0) {
-      int gkb = 0;  // stages issued so far (all tiles)
+      int& gkb = gkb_issued;
       bool aborted = false;
       unsigned int next = blockIdx.x;  // static walk when no tile counter is given
       for (int i = 0; !aborted; ++i) {
         const int slot = i % RING;
-        if (!mbar_wait(ring_empty(slot), (uint32_t)(((i / RING) & 1) ^ 1), abort_flag)) {
+        if (!mbar_wait(ring_empty(slot), (uint32_t)(((i / RING) & 1) ^ 1), abort_flag, a.wait_ns)) {
           signal_abort(abort_flag);
           break;
         }
@@ -831,10 +846,14 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         for (int kb = 0; kb < nkb; ++kb) {
           const int st = gkb % STAGES;
           const uint32_t ph = (uint32_t)((gkb / STAGES) & 1);
-          if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag)) {
+          if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag, a.wait_ns)) {
             signal_abort(abort_flag);
             aborted = true;
             break;
+          }
+          if (gkb == a.withhold && blockIdx.x == 0) {
+            ++gkb;  // test hook: this stage never arrives
+            continue;
           }
           mbar_expect_tx(full_bar(st), stage_bytes);
           const uint32_t sa = sbase + st * stage_bytes;
@@ -853,10 +872,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           ++gkb;
         }
       }
-      if (*abort_flag) {
-        for (int k = gkb > STAGES ? gkb - STAGES : 0; k < gkb; ++k)
-          mbar_wait(full_bar(k % STAGES), (uint32_t)((k / STAGES) & 1), nullptr);
-      }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -865,7 +880,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
       bool aborted = false;
       for (int i = 0; !aborted; ++i) {
         const int slot = i % RING;
-        if (!mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag)) {
+        if (!mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a.wait_ns)) {
           signal_abort(abort_flag);
           break;
         }
@@ -880,7 +895,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         bool f_started = false;
         for (int kb = 0; kb < nkb; ++kb) {
           const int st = gkb % STAGES;
-          if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag)) {
+          if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag, a.wait_ns)) {
             signal_abort(abort_flag);
             aborted = true;
             break;
@@ -894,7 +909,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           // epilogue has taken everything out of TMEM; inside a tile the FP32
           // group may run ahead while the exact groups drain
           if (first && gch > 0 && (c == 0 || g.fdrain)) {
-            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag)) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a.wait_ns)) {
               signal_abort(abort_flag);
               aborted = true;
               break;
@@ -904,7 +919,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           if (g.fdrain && first) f_started = false;
           if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
           if (!g.fdrain && first && c > 0) {
-            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag)) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a.wait_ns)) {
               signal_abort(abort_flag);
               aborted = true;
               break;
@@ -935,7 +950,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
     int gch = 0;
     for (int i = 0;; ++i) {
       const int slot = i % RING;
-      const bool got = mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag);
+      const bool got = mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a.wait_ns);
       if (!got) signal_abort(abort_flag);
       const int t = got ? ring[slot] : -1;
       __syncwarp();
@@ -988,7 +1003,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
       for (int j = 0; j < CW; ++j) R[j] = 0;
       bool ok = true;
       for (int c = 0; c < nchunks; ++c) {
-        const bool got = mbar_wait(accfull_bar, (uint32_t)(gch & 1), abort_flag);
+        const bool got = mbar_wait(accfull_bar, (uint32_t)(gch & 1), abort_flag, a.wait_ns);
         if (!__all_sync(0xffffffffu, got)) {
           signal_abort(abort_flag);
           ok = false;
@@ -1071,8 +1086,13 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   }
 
   __syncthreads();
+  // after an abort, the producer's copies land before the CTA exits
+  if (warp == 0 && lane == 0 && *abort_flag) {
+    for (int k = gkb_issued > STAGES ? gkb_issued - STAGES : 0; k < gkb_issued; ++k)
+      mbar_wait(full_bar(k % STAGES), (uint32_t)((k / STAGES) & 1), nullptr, a.wait_ns);
+  }
   if (warp == 1) {
-    if (*abort_flag) mbar_wait(done_bar, 0, nullptr);
+    if (*abort_flag) mbar_wait(done_bar, 0, nullptr, a.wait_ns);
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::TMEM_COLS) : "memory");
   }
@@ -1173,16 +1193,18 @@ GroupedFn grouped_kernel_for(int S, int BN) {
   return BN == 32 ? grouped_for<32>(S) : BN == 64 ? grouped_for<64>(S) : grouped_for<128>(S);
 }
 
-// Opt every instantiation in to its dynamic shared memory once per device.
+// Opt every instantiation in to its dynamic shared memory once per device
+// context (again after a cudaDeviceReset, whose new context has a new id).
 int g_num_sms[64] = {0};
 
 int configure_device() {
   static std::mutex mu;
-  static int configured[64] = {0};
+  static unsigned long long configured[64] = {0};  // context id configured on each device
   int dev = 0;
   GB_TRY(cuda_status(cudaGetDevice(&dev), "cudaGetDevice"));
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lk(mu);
-  if (dev < 0 || dev >= 64 || configured[dev]) return GB_OK;
+  if (dev < 0 || dev >= 64 || (ctx != 0 && configured[dev] == ctx)) return GB_OK;
   for (int bn : {32, 64, 128})
     for (int sl : {1, 2, 3, 4, 5, 6, SPLIT_TF32X3}) {
       const int sm = (int)smem_bytes(sl, bn);
@@ -1198,7 +1220,7 @@ int configure_device() {
                        "cudaFuncSetAttribute"));
   GB_TRY(cuda_status(cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev),
                      "cudaDeviceGetAttribute"));
-  configured[dev] = 1;
+  configured[dev] = current_context_id();
   return GB_OK;
 }
 
@@ -1240,8 +1262,12 @@ int check_problem(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
   return GB_OK;
 }
 
+constexpr unsigned long long kDefaultWaitNs = 2000000000ull;  // 2 s per wait
+std::atomic<unsigned long long> g_wait_limit_ns{kDefaultWaitNs};
+std::atomic<int> g_withhold_stage{-1};
+
 KArgs make_args(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g) {
-  KArgs ka{g, A, B, frac_bits(g.S, g.K)};
+  KArgs ka{g, A, B, frac_bits(g.S, g.K), g_wait_limit_ns.load(), g_withhold_stage.load()};
   if (g.K > 4096 && g.S != SPLIT_TF32X3) ka.g.fdrain = 1;
   return ka;
 }
@@ -1347,6 +1373,51 @@ int ozaki_status(int reset, int* out) {
   return GB_OK;
 }
 
+int* device_status_word() {
+  static std::mutex mu;
+  static unsigned long long ctx_ids[64] = {0};
+  static int* addrs[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  const unsigned long long id = current_context_id();
+  std::lock_guard<std::mutex> lk(mu);
+  if (addrs[dev] == nullptr || id == 0 || ctx_ids[dev] != id) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_tc_status) != cudaSuccess) return nullptr;
+    addrs[dev] = static_cast<int*>(p);
+    ctx_ids[dev] = current_context_id();
+  }
+  return addrs[dev];
+}
+
+// The two driver functions come through the runtime's entry-point query, so
+// the library keeps no link-time dependency on the driver library (it loads
+// on a machine without a GPU, where only its size queries are used).
+unsigned long long current_context_id() {
+  using GetCurrentFn = CUresult (*)(CUcontext*);
+  using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(f);
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 int ozaki_kernel_info(char* out, size_t len) {
   cudaFuncAttributes fa{};
   cudaError_t e = cudaFuncGetAttributes(&fa, kernel_for(6, 128));
@@ -1366,3 +1437,15 @@ int ozaki_kernel_info(char* out, size_t len) {
 }
 
 }  // namespace gb
+
+extern "C" int gb_set_wait_limit_ns(unsigned long long limit_ns) {
+  gb::clear_error();
+  gb::g_wait_limit_ns.store(limit_ns ? limit_ns : gb::kDefaultWaitNs);
+  return GB_OK;
+}
+
+extern "C" int gb_test_withhold_stage(int stage) {
+  gb::clear_error();
+  gb::g_withhold_stage.store(stage < 0 ? -1 : stage);
+  return GB_OK;
+}

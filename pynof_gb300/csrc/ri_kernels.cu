@@ -27,8 +27,11 @@ __global__ void contract_diag_kernel(const double* __restrict__ C, const double*
 // consecutive l; the exponent field's maximum over them comes from one warp
 // reduction per n and lands in lane n % 32, which folds it in with atomicMax
 // every 32 n.
+// A NaN or an infinity in T (exponent field 0x7FF) is reported in the status
+// word, as the slicer does for the rows it measures.
 __global__ void contract_diag_exps_kernel(const double* __restrict__ C, const double* __restrict__ T,
-                                          double* __restrict__ d, int* __restrict__ texps, int N, int P, int Q) {
+                                          double* __restrict__ d, int* __restrict__ texps, int N, int P, int Q,
+                                          int* status) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   const int q = blockIdx.y;
   const int lane = threadIdx.x & 31;
@@ -47,7 +50,10 @@ __global__ void contract_diag_exps_kernel(const double* __restrict__ C, const do
       const unsigned int mx = __reduce_max_sync(0xffffffffu, ex);
       if (lane == j) mine = mx;
     }
-    if (lane < nn) atomicMax(eq + n0 + lane, (int)(mine > 1u ? mine : 1u) - 1022);
+    if (lane < nn) {
+      atomicMax(eq + n0 + lane, (int)(mine > 1u ? mine : 1u) - 1022);
+      if (mine == 0x7FFu && status) atomicCAS(status, 0, GB_ERR_NONFINITE);
+    }
   }
   if (in) d[(long long)q * Q + l] = acc;
 }
@@ -152,7 +158,8 @@ int launch_contract_diag(const double* C, const double* T, double* d, int N, int
     // every entry below any exponent folded in (0x80808080 < -1021)
     GB_TRY(cuda_status(cudaMemsetAsync(texps, 0x80, sizeof(int) * (size_t)P * N, s), "contract_diag exponents"));
     GB_LAUNCH("contract_diag", s,
-              contract_diag_exps_kernel<<<dim3(cdiv(Q, 128), P), 128, 0, s>>>(C, T, d, texps, N, P, Q));
+              contract_diag_exps_kernel<<<dim3(cdiv(Q, 128), P), 128, 0, s>>>(C, T, d, texps, N, P, Q,
+                                                                               device_status_word()));
     return GB_OK;
   }
   GB_LAUNCH("contract_diag", s, contract_diag_kernel<<<dim3(cdiv(Q, 128), P), 128, 0, s>>>(C, T, d, N, P, Q));

@@ -41,8 +41,15 @@ __device__ __forceinline__ void make_digits(double x, int E, unsigned short* out
   out[0] = (unsigned short)(__float_as_uint(f1) >> 16);
 }
 
+// A NaN or an infinity has the largest magnitude bits of all; it has no digits,
+// so the row that holds one is reported in the status word (the first error
+// recorded there stays) and the split-product kernels refuse to start.
+__device__ __forceinline__ void note_nonfinite(unsigned long long maxbits, int* status) {
+  if (maxbits >= 0x7FF0000000000000ull && status) atomicCAS(status, 0, GB_ERR_NONFINITE);
+}
+
 // One warp per row; K is the unit-stride index.
-__global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps) {
+__global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps, int* status) {
   const long long b = blockIdx.y;
   const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -58,11 +65,14 @@ __global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restri
     const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
     mx = v > mx ? v : mx;
   }
-  if (lane == 0) exps[b * rows + row] = exponent_of(mx);
+  if (lane == 0) {
+    exps[b * rows + row] = exponent_of(mx);
+    note_nonfinite(mx, status);
+  }
 }
 
 // One thread per row; rows are the unit-stride index.
-__global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps) {
+__global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps, int* status) {
   const long long b = blockIdx.y;
   const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= rows) return;
@@ -73,6 +83,7 @@ __global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restri
     mx = v > mx ? v : mx;
   }
   exps[b * rows + row] = exponent_of(mx);
+  note_nonfinite(mx, status);
 }
 
 // One CTA of 256 threads per (row block, k block): thread -> (row r, k group of
@@ -210,11 +221,15 @@ int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s, bo
   if (exps_ready) {
     GB_REQUIRE(dst.kind == 0, GB_ERR_INVALID_ARG, "slice_operand: recorded exponents are for digit slices");
   } else if (src.kfast) {
+    int* st = device_status_word();
     GB_LAUNCH("slice_rowexp", s,
-              rowexp_kfast_kernel<<<dim3(cdiv(dst.rows, 8), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K, dst.exps));
+              rowexp_kfast_kernel<<<dim3(cdiv(dst.rows, 8), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K, dst.exps,
+                                                                                    st));
   } else {
+    int* st = device_status_word();
     GB_LAUNCH("slice_rowexp", s,
-              rowexp_rfast_kernel<<<dim3(cdiv(dst.rows, 256), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K, dst.exps));
+              rowexp_rfast_kernel<<<dim3(cdiv(dst.rows, 256), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K,
+                                                                                      dst.exps, st));
   }
   const long long blocks = (long long)dst.rblocks() * dst.kblocks();
   GB_REQUIRE(blocks <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many blocks");

@@ -21,6 +21,7 @@ GPU_FUNCTIONS = {
     "integrals.Integrals_MO_RI_GPU": integrals.Integrals_MO_RI_GPU,
     "integrals.Integrals_MO_Full_GPU": integrals_full.Integrals_MO_Full_GPU,
     "utils.computeF_RC_GPU": utils.computeF_RC_GPU,
+    "utils.computeF_RO_GPU": utils.computeF_RO_GPU,
     "integrals.JK_HF_Full_GPU": integrals_hf.JK_HF_Full_GPU,
     "integrals.JKalpha_HF_Full_GPU": integrals_hf.JKalpha_HF_Full_GPU,
     "integrals.iajb_Full_GPU": integrals_full.iajb_Full_GPU,

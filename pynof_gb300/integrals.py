@@ -68,7 +68,9 @@ def as_device(x) -> torch.Tensor:
 
 
 def to_host(*tensors):
-    """Copy device tensors into pinned host memory and return numpy arrays.
+    """Copy device tensors into pinned host memory and return numpy arrays;
+    raise GBError if the device status word reports a failed split-product
+    kernel or a non-finite operand.
 
     Pinned blocks come from torch's caching host allocator, so repeated calls
     of the same size reuse the same page-locked memory once the caller drops
@@ -79,6 +81,9 @@ def to_host(*tensors):
         h.copy_(t, non_blocking=True)
         outs.append(h)
     torch.cuda.current_stream().synchronize()
+    # a split-product kernel that gave up, or a non-finite operand, must not
+    # hand back unwritten memory as results
+    ops.check_device_status()
     res = tuple(h.numpy() for h in outs)
     return res if len(res) > 1 else res[0]
 

@@ -244,6 +244,23 @@ def fock_rc(J, K, n, H, cj12, ck12, nbeta: int, nalpha: int, no1: int = 0):
     return F
 
 
+def fock_ro(J, K, n, H, cj12, ck12, nbeta: int, nalpha: int, no1: int = 0):
+    """F (nbf5, nbf, nbf), restricted open shell (computeF_RO)."""
+    P, N, _ = J.shape
+    _require(J, (P, N, N), "J")
+    _require(K, (P, N, N), "K")
+    _require(n, (P,), "n")
+    _require(H, (N, N), "H")
+    _require(cj12, (P, P), "cj12")
+    _require(ck12, (P, P), "ck12")
+    dev = J.device
+    F = torch.empty((P, N, N), dtype=_F64, device=dev)
+    wp, wn = _ws("gb_fock_ro_workspace_f64", N, P, device=dev)
+    _lib.call("gb_fock_ro_f64", _ptr(J), _ptr(K), _ptr(n), _ptr(H), _ptr(cj12), _ptr(ck12), N, P, nbeta, nalpha, no1,
+              _ptr(F), wp, wn, _stream(dev))
+    return F
+
+
 def lagrange(F, C, noptorb: int | None = None):
     """elag (nbf, nbf) from the generalized Fock matrices (computeLagrange)."""
     P, N, _ = F.shape
@@ -389,11 +406,29 @@ class AntisymNorm:
 # ----------------------------------------------------------------------------
 # split-product tensor-core path
 # ----------------------------------------------------------------------------
-def check_device_status() -> None:
-    """Raise if a tensor-core kernel recorded a timeout (synchronises)."""
-    st = _lib.device_status(reset=True)
+_STATUS_MESSAGES = {
+    5: "a tensor-core kernel gave up on a bounded wait; its outputs (and those of every split-product call "
+       "since) are not valid",
+    6: "an operand of a split-product call held a NaN or an infinity; the outputs are not valid",
+}
+
+
+def check_device_status(reset: bool = False) -> None:
+    """Raise GBError if a tensor-core kernel recorded an error on the current
+    device (GB_ERR_TIMEOUT, GB_ERR_NONFINITE).  Synchronises the device.
+
+    The status word is shared by every caller on the device and stays set
+    until :func:`reset_device_status` (or ``reset=True`` here) clears it, so a
+    failure is reported to every caller that checks after its own work rather
+    than to whichever checks first."""
+    st = _lib.device_status(reset=reset)
     if st != 0:
-        raise _lib.GBError(st, "a tensor-core kernel gave up on a bounded wait")
+        raise _lib.GBError(st, _STATUS_MESSAGES.get(st, "tensor-core status word is set"))
+
+
+def reset_device_status() -> int:
+    """Clear the tensor-core status word; returns what it held."""
+    return _lib.device_status(reset=True)
 
 
 #: Split code of the three-product TF32 form (``GB_SPLIT_TF32X3``), accepted
@@ -504,6 +539,7 @@ def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int =
         with torch.cuda.stream(cs):
             Kh[q0:q1].copy_(K[q0:q1], non_blocking=True)
     cs.synchronize()
+    check_device_status()
     return Jh.numpy(), Kh.numpy()
 
 

@@ -74,6 +74,9 @@ class Backend:
     def _sync_host(self, *ts):
         with torch.cuda.stream(self.stream):
             out = [t.to("cpu", non_blocking=False) for t in ts]
+        # after this stream's work: a timed-out or non-finite split-product
+        # call raises here instead of feeding unwritten results to the loop
+        ops.check_device_status()
         return [o.numpy() for o in out]
 
     # device-side pieces (current stream = self.stream)

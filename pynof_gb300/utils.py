@@ -1,12 +1,12 @@
 """Drop-in mirror of PyNOF's Fock / Lagrangian / energy functions
 (``pynof/utils.py``) for the device path.
 
-Side effects follow the reference: ``computeLagrange2`` and ``computeF_RC_GPU``
-zero the diagonals of the caller's ``cj12`` / ``ck12`` in place
-(``utils.py:46,51,77,81,269-270``).  Open-shell (MSpin != 0) inputs are
-rejected where the reference has a restricted-open-shell branch this path
-does not implement (``computeF_RO``); ``computeLagrange2`` returns a zero
-Lagrangian for them exactly as the reference does.
+Side effects follow the reference: ``computeLagrange2``, ``computeF_RC_GPU``
+and ``computeF_RO_GPU`` zero the diagonals of the caller's ``cj12`` / ``ck12``
+in place (``utils.py:46,51,77,81,120,138,269-270``).  For open shells
+(MSpin != 0) ``ENERGY1r``'s no1 > 0 route takes the restricted open-shell
+Fock (``computeF_RO``), and ``computeLagrange2`` returns a zero Lagrangian
+exactly as the reference does.
 """
 from __future__ import annotations
 
@@ -61,6 +61,22 @@ def computeF_RC_driver(J, K, n, H, cj12, ck12, p):
     return computeF_RC_GPU(J, K, n, H, cj12, ck12, p)
 
 
+def computeF_RO_GPU(J, K, n, H, cj12, ck12, p):
+    """F (nbf5, nbf, nbf) host numpy, restricted open shell --
+    ``pynof/utils.py:172-246``."""
+    ini = p.no1 if p.no1 > 1 else 0
+    _zero_diag(cj12, ini)
+    _zero_diag(ck12, ini)
+    F = ops.fock_ro(as_device(J), as_device(K), as_device(n), as_device(H), as_device(cj12), as_device(ck12),
+                    p.nbeta, p.nalpha, p.no1)
+    return to_host(F)
+
+
+def computeF_RO_driver(J, K, n, H, cj12, ck12, p):
+    """``pynof/utils.py:87-94`` for the device path."""
+    return computeF_RO_GPU(J, K, n, H, cj12, ck12, p)
+
+
 def rotate_orbital(y, C, p):
     """``pynof/utils.py:550-565``: C expm(Y) from the packed step y, on the
     device in FP64 (the reference builds Y in a Python loop and calls
@@ -84,8 +100,6 @@ def energy1r_device(C, n, H, I, b_mnl, cj12, ck12, p):
         P = p.nbf5
         E = torch.trace(elag[:P, :P]) + torch.dot(dn[:P], torch.diagonal(Hmat)[:P])
         return float(E), elag
-    if p.MSpin != 0:
-        raise NotImplementedError("restricted open-shell Fock (computeF_RO) is not on the device path")
     ini = p.no1 if p.no1 > 1 else 0
     _zero_diag(cj12, ini)
     _zero_diag(ck12, ini)
@@ -93,7 +107,8 @@ def energy1r_device(C, n, H, I, b_mnl, cj12, ck12, p):
         J, K = jkj_ri_device(dC, b_mnl, p.nbf5)
     else:
         J, K = ops.jkj_full(dC, as_device(I), p.nbf5)
-    F = ops.fock_rc(J, K, dn, dH, as_device(cj12), as_device(ck12), p.nbeta, p.nalpha, p.no1)
+    fock = ops.fock_rc if p.MSpin == 0 else ops.fock_ro
+    F = fock(J, K, dn, dH, as_device(cj12), as_device(ck12), p.nbeta, p.nalpha, p.no1)
     elag = ops.lagrange(F, dC, p.noptorb)
     E = ops.energy_elec(elag, dC, dH, dn, p.nbeta, p.nalpha, p.HighSpin)
     return float(E), elag

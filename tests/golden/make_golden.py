@@ -46,6 +46,10 @@ CASES = {
 #: outer iterations of the reference's solve loop recorded for the loop parity test
 LOOP_CASE = ("water", 0, 3)
 
+#: restricted open shell (two singly occupied orbitals, two inactive ones):
+#: the computeF_RO route of ENERGY1r (utils.py:423-425)
+OPEN_SHELL = dict(nbf=30, nbfaux=120, no1=2, ndoc=3, ncwo=3, nsoc=2, MSpin=1)
+
 
 def run_loop(pynof, workload, seed, n_outer):
     """The body of compute_energy's loop (energy.py:94-153) with the
@@ -241,13 +245,65 @@ def run_case(pynof, name, workload, seed, full, jit):
     return out, meta
 
 
+def run_open_shell(pynof, seed=5):
+    """computeF_RO_CPU, computeLagrange, computeE_elec (both HighSpin
+    settings) and ENERGY1r with no1 > 0 and MSpin != 0, on seeded inputs with
+    GNOF coefficients from the reference's PNOFi_selector."""
+    st = synthetic.Structure(**OPEN_SHELL)
+    b, C, H, _ = synthetic.make_inputs(st, seed)
+    p = make_param(st)
+    P, nb, na = st.nbf5, st.nbeta, st.nalpha
+    rng = np.random.Generator(np.random.PCG64(seed + 200))
+    n = np.zeros(P)
+    n[: st.no1] = 1.0
+    n[st.no1:nb] = np.sort(rng.uniform(0.6, 0.99, st.ndoc))[::-1]
+    n[nb:na] = 0.5
+    n[na:] = np.sort(rng.uniform(0.001, 0.2, P - na))[::-1]
+    cj12, ck12 = pynof.PNOFi_selector(n, p)
+    out = dict(b=b, C=C, H=H, n=n, cj12=cj12.copy(), ck12=ck12.copy())
+    J, K = pynof.computeJKj(C, [], b, p)
+    out.update(J_ri=J, K_ri=K)
+    cj, ck = cj12.copy(), ck12.copy()
+    F = pynof.computeF_RO_CPU(J, K, n, H, cj, ck, p)
+    out.update(F_ro=F, cj12_zeroed=cj, ck12_zeroed=ck)
+    elag = pynof.computeLagrange(F, C, p)
+    out.update(elag_F=elag, E_F=np.array(pynof.computeE_elec(H, C, n, elag, p)))
+    ph = make_param(st, HighSpin=True)
+    out.update(E_F_highspin=np.array(pynof.computeE_elec(H, C, n, elag, ph)))
+    E, el1, sd, md = pynof.ENERGY1r(C, n, H, [], b, cj12.copy(), ck12.copy(), p)
+    out.update(E1r=np.array(E), elag1r=el1, sumdiff1r=np.array(sd), maxdiff1r=np.array(md))
+    meta = dict(case="open_shell", seed=seed, sizes=OPEN_SHELL, numpy=np.__version__,
+                checks={"E1r_vs_fock_route": abs(float(E) - float(out["E_F"]))})
+    return out, meta
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--only", default=None, help="write just this fixture (a case name, 'loop' or 'open_shell')")
     args = ap.parse_args()
     pynof = import_reference(args.ref)
+    meta_path = os.path.join(args.out, "golden_meta.json")
+    if args.only:
+        with open(meta_path) as f:
+            allmeta = json.load(f)
+        if args.only == "open_shell":
+            out, meta = run_open_shell(pynof)
+        elif args.only in CASES:
+            out, meta = run_case(pynof, args.only, *CASES[args.only])
+        else:
+            raise SystemExit(f"unknown fixture {args.only!r}")
+        np.savez_compressed(os.path.join(args.out, f"{args.only}.npz"), **out)
+        allmeta[args.only] = meta
+        print(args.only, json.dumps(meta["checks"]))
+        with open(meta_path, "w") as f:
+            json.dump(allmeta, f, indent=1, sort_keys=True)
+        return
     allmeta = {}
+    out, meta = run_open_shell(pynof)
+    np.savez_compressed(os.path.join(args.out, "open_shell.npz"), **out)
+    allmeta["open_shell"] = meta
     for name, (workload, seed, full, jit) in CASES.items():
         out, meta = run_case(pynof, name, workload, seed, full, jit)
         np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
@@ -259,7 +315,7 @@ def main():
     allmeta["loop_water"] = dict(workload=wl, seed=seed, n_outer=n_outer, E_orb=loop["E_orb"].tolist(),
                                  g_orb=loop["g_orb"].tolist(), g_occ=loop["g_occ"].tolist())
     print("loop", allmeta["loop_water"])
-    with open(os.path.join(args.out, "golden_meta.json"), "w") as f:
+    with open(meta_path, "w") as f:
         json.dump(allmeta, f, indent=1, sort_keys=True)
 
 

@@ -140,3 +140,50 @@ def test_post_nof_transforms_golden(torch_cuda, name):
     assert nrel(integrals_full.compute_iajb(g["C"], I, None, p), g["iajb"]) < 1e-10
     assert nrel(integrals_full.compute_pqrt(g["C"], I, None, p), g["pqrt"]) < 1e-10
 
+
+
+def _open_shell_param(**over):
+    import json
+    import os
+
+    from conftest import GOLDEN
+    from pynof_gb300 import synthetic
+
+    with open(os.path.join(GOLDEN, "golden_meta.json")) as f:
+        st = synthetic.Structure(**json.load(f)["open_shell"]["sizes"])
+    for k, v in over.items():
+        setattr(st, k, v)
+    return st
+
+
+def test_open_shell_fock_route(torch_cuda):
+    """computeF_RO (utils.py:172-246), computeLagrange, computeE_elec (both
+    HighSpin settings) and ENERGY1r's no1 > 0, MSpin != 0 route, RI and
+    full ERI, FP64 and split products, against the reference's outputs."""
+    from pynof_gb300 import integrals, ops, utils
+
+    g = load_golden("open_shell")
+    p = _open_shell_param()
+    cj, ck = g["cj12"].copy(), g["ck12"].copy()
+    F = utils.computeF_RO_GPU(g["J_ri"], g["K_ri"], g["n"], g["H"], cj, ck, p)
+    assert nrel(F, g["F_ro"]) < TOL
+    assert np.array_equal(cj, g["cj12_zeroed"]) and np.array_equal(ck, g["ck12_zeroed"])
+    dC, dH, dn = ops.to_device(g["C"]), ops.to_device(g["H"]), ops.to_device(g["n"])
+    elag = ops.lagrange(ops.to_device(F), dC, p.noptorb)
+    assert nrel(elag.cpu().numpy(), g["elag_F"]) < TOL
+    for hs, key in ((False, "E_F"), (True, "E_F_highspin")):
+        E = float(ops.energy_elec(elag, dC, dH, dn, p.nbeta, p.nalpha, hs))
+        assert abs(E - float(g[key])) < TOL * abs(float(g[key])), key
+    db = ops.to_device(g["b"])
+    I = integrals.upload_integrals(np.einsum("mnQ,slQ->mnsl", g["b"], g["b"]), None)[0]
+    pf = _open_shell_param(RI=False)
+    for mode in ("fp64", "mixed"):
+        integrals.set_precision(mode, 6)
+        try:
+            for pp, ints in ((p, (None, db)), (pf, (I, None))):
+                E1, el1, sd, md = utils.ENERGY1r(g["C"], g["n"], g["H"], ints[0], ints[1], g["cj12"].copy(),
+                                                 g["ck12"].copy(), pp)
+                assert abs(E1 - float(g["E1r"])) < TOL * abs(E1), (mode, pp.RI)
+                assert nrel(el1, g["elag1r"]) < TOL, (mode, pp.RI)
+        finally:
+            integrals.set_precision("mixed", 6)

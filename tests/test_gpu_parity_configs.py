@@ -1,0 +1,183 @@
+"""Parity at the medium and the nbf=600 workloads, against the oracle.
+
+* nbf=300, naux=1200, nbf5=150 (seed 0): the FP64 RI path (computeJKj,
+  computeJKH_MO, computeLagrange2) against the oracle at 1e-10 normwise, and
+  the full-ERI path on I = b b^T (built on the device, 64.8 GB, 8-fold
+  symmetric) against the oracle's RI results: for that I the two routes are
+  the same mathematics (``integrals.py:197-218, 332-362``), so the RI oracle
+  is the full-ERI oracle without a 64.8 GB host tensor.
+* nbf=600, naux=2400, nbf5=300 (seed 0): the FP64 DMMA path and the 6-slice
+  split-product tensor-core path against the oracle at 1e-10 normwise, and
+  the energies E = tr elag[:P, :P] + sum_i n_i Hmat_ii (computeLagrange2)
+  and E from J_i, K_i (computeF_RC -> computeLagrange -> computeE_elec) to
+  1e-10 relative (FP64) and 1 micro-Hartree (split products).
+
+Tolerances are normwise, max|gpu - ref| / max|ref| (see conftest.nrel).
+"""
+import numpy as np
+import pytest
+
+from conftest import nrel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+E_TOL_MIXED = 1e-6  # Hartree
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _coefficients(n, st):
+    from pynof_gb300 import nof
+
+    cj, ck = nof.cjckd8(n, st)
+    np.fill_diagonal(cj, 0.0)
+    np.fill_diagonal(ck, 0.0)
+    return cj, ck
+
+
+def _energy_lagrange2(elag, Hmat, n, P):
+    return float(np.trace(elag[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat)[:P]))
+
+
+def _energy_jk(J, K, C, H, n, cj, ck):
+    """tr(C_i^T F_i C_i) + sum_i n_i H_ii with the closed-shell generalized
+    Fock F_i = n_i H + n_i J_i + sum_j cj_ij J_j - sum_j ck_ij K_j (no1 = 0,
+    zero diagonals of cj, ck): computeF_RC -> computeLagrange -> computeE_elec."""
+    P = J.shape[0]
+    Cp = C[:, :P]
+    Hd = np.einsum("mi,mi->i", Cp, H @ Cp)
+    Jd = np.einsum("mi,jmi->ji", Cp, np.matmul(J, Cp))  # [j, i] = C_i^T J_j C_i
+    Kd = np.einsum("mi,jmi->ji", Cp, np.matmul(K, Cp))
+    return float(2.0 * np.dot(n, Hd) + np.dot(n, np.diagonal(Jd)) + np.sum(cj * Jd.T) - np.sum(ck * Kd.T))
+
+
+@pytest.fixture(scope="module")
+def c2(torch_cuda):
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import ops, synthetic
+
+    st = synthetic.structure("c2")
+    b, C, H, n = synthetic.make_inputs(st, 0)
+    P = st.nbf5
+    cj, ck = _coefficients(n, st)
+    ref = {
+        "jk": orc.jkj_ri(C, b, P),
+        "mo": orc.jkh_mo_ri(C, H, b, P),
+        "l2": orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st),
+    }
+    dev = {"b": ops.to_device(b), "C": ops.to_device(C), "H": ops.to_device(H), "n": ops.to_device(n),
+           "cj": ops.to_device(cj), "ck": ops.to_device(ck)}
+    return st, (b, C, H, n, cj, ck), ref, dev
+
+
+def test_c2_ri_fp64_vs_oracle(c2):
+    from pynof_gb300 import ops
+
+    st, host, ref, d = c2
+    P = st.nbf5
+    J, K = ops.jkj_ri(d["C"], d["b"], P)
+    assert nrel(J.cpu().numpy(), ref["jk"][0]) < TOL
+    assert nrel(K.cpu().numpy(), ref["jk"][1]) < TOL
+    a, b_, c = ops.jkh_mo_ri(d["C"], d["H"], d["b"], P)
+    for got, want in zip((a, b_, c), ref["mo"]):
+        assert nrel(got.cpu().numpy(), want) < TOL
+    el, Hm = ops.lagrange2_ri(d["C"], d["H"], d["b"], d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)
+    assert nrel(el.cpu().numpy(), ref["l2"][0]) < TOL
+    assert nrel(Hm.cpu().numpy(), ref["l2"][1]) < TOL
+
+
+def test_c2_full_eri_vs_ri_oracle(c2, torch_cuda):
+    """JKj_Full, JKH_MO_Full and the full-ERI Lagrangian over I = b b^T
+    (64.8 GB FP64 on the device) against the oracle's RI outputs."""
+    from pynof_gb300 import ops
+
+    torch = torch_cuda
+    st, host, ref, d = c2
+    N, Q, P = st.nbf, st.nbfaux, st.nbf5
+    B = d["b"].reshape(N * N, Q)
+    I = torch.matmul(B, B.T).reshape(N, N, N, N)
+    try:
+        J, K = ops.jkj_full(d["C"], I, P)
+        ej, ek = nrel(J.cpu().numpy(), ref["jk"][0]), nrel(K.cpu().numpy(), ref["jk"][1])
+        del J, K
+        a, b_, c = ops.jkh_mo_full(d["C"], d["H"], I, P)
+        emo = [nrel(got.cpu().numpy(), want) for got, want in zip((a, b_, c), ref["mo"])]
+        del a, b_, c
+        el, Hm = ops.lagrange2_full(d["C"], d["H"], I, d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)
+        el_err, hm_err = nrel(el.cpu().numpy(), ref["l2"][0]), nrel(Hm.cpu().numpy(), ref["l2"][1])
+        del el, Hm
+    finally:
+        del I
+        ops.POOL.clear()
+        torch.cuda.empty_cache()
+    print(f"c2 full ERI: J {ej:.2e} K {ek:.2e} J_MO/K_MO/H_core {emo} elag {el_err:.2e}")
+    assert ej < TOL and ek < TOL
+    assert max(emo) < TOL
+    assert el_err < TOL and hm_err < TOL
+
+
+@pytest.fixture(scope="module")
+def c3(torch_cuda):
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import ops, synthetic
+
+    st = synthetic.structure("c3")
+    b, C, H, n = synthetic.make_inputs(st, 0)
+    P = st.nbf5
+    cj, ck = _coefficients(n, st)
+    Jr, Kr = orc.jkj_ri(C, b, P)
+    ref = {
+        "jk": (Jr, Kr),
+        "E_jk": _energy_jk(Jr, Kr, C, H, n, cj, ck),
+        "mo": orc.jkh_mo_ri(C, H, b, P),
+        "l2": orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st),
+    }
+    ref["E_l2"] = _energy_lagrange2(ref["l2"][0], ref["l2"][1], n, P)
+    dev = {"b": ops.to_device(b), "C": ops.to_device(C), "H": ops.to_device(H), "n": ops.to_device(n),
+           "cj": ops.to_device(cj), "ck": ops.to_device(ck)}
+    yield st, (b, C, H, n, cj, ck), ref, dev
+    del dev
+    ops.POOL.clear()
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed_s6"])
+def test_c3_vs_oracle(c3, torch_cuda, form):
+    from pynof_gb300 import ops
+
+    torch = torch_cuda
+    st, (b, C, H, n, cj, ck), ref, d = c3
+    P = st.nbf5
+    if form == "fp64":
+        J, K = ops.jkj_ri(d["C"], d["b"], P)
+        mo = ops.jkh_mo_ri(d["C"], d["H"], d["b"], P)
+        el, Hm = ops.lagrange2_ri(d["C"], d["H"], d["b"], d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)
+        e_tol = TOL * abs(ref["E_l2"])
+    else:
+        prep = ops.PreparedRI(d["b"], 6)
+        J, K = ops.jkj_ri_mixed(d["C"], prep, P)
+        mo = ops.jkh_mo_ri_mixed(d["C"], d["H"], prep, P)
+        el, Hm = ops.lagrange2_ri_mixed(d["C"], d["H"], prep, d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)
+        ops.check_device_status()
+        del prep
+        e_tol = E_TOL_MIXED
+    Jh, Kh = J.cpu().numpy(), K.cpu().numpy()
+    del J, K
+    errs = {"J": nrel(Jh, ref["jk"][0]), "K": nrel(Kh, ref["jk"][1])}
+    errs.update({k: nrel(v.cpu().numpy(), w) for k, v, w in zip(("J_MO", "K_MO", "H_core"), mo, ref["mo"])})
+    elh, Hmh = el.cpu().numpy(), Hm.cpu().numpy()
+    errs["elag"] = nrel(elh, ref["l2"][0])
+    errs["Hmat"] = nrel(Hmh, ref["l2"][1])
+    dE_l2 = abs(_energy_lagrange2(elh, Hmh, n, P) - ref["E_l2"])
+    dE_jk = abs(_energy_jk(Jh, Kh, C, H, n, cj, ck) - ref["E_jk"])
+    torch.cuda.empty_cache()
+    print(f"c3 {form}: " + " ".join(f"{k} {v:.2e}" for k, v in errs.items()) +
+          f" |dE| lagrange2 {dE_l2:.2e} jk {dE_jk:.2e} Eh (E = {ref['E_l2']:.6f}, {ref['E_jk']:.6f})")
+    bad = {k: v for k, v in errs.items() if not v < TOL}
+    assert not bad, bad
+    assert dE_l2 < e_tol and dE_jk < max(e_tol, TOL * abs(ref["E_jk"]))

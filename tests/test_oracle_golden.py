@@ -5,12 +5,14 @@ The fixtures were produced by running the reference functions
 restatement.  Agreement is required to 1e-12 normwise (BLAS summation order is
 the only difference).
 """
+import json
+import os
 import types
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden, nrel, param_for
+from conftest import GOLDEN, GOLDEN_CASES, load_golden, nrel, param_for
 from oracle import pynof_oracle as orc
 
 TOL = 1e-12
@@ -129,3 +131,35 @@ def test_post_nof_transforms(name):
     occ, vir, full = (p.no1, p.nalpha), (p.nalpha, p.nbf), (0, p.nbf)
     assert nrel(orc.mo4_full(g["C"], I, occ, vir, occ, vir), g["iajb"]) < TOL
     assert nrel(orc.mo4_full(g["C"], I, full, full, full, full), g["pqrt"]) < TOL
+
+
+def open_shell_param(**over):
+    from pynof_gb300 import synthetic
+
+    with open(os.path.join(GOLDEN, "golden_meta.json")) as f:
+        sizes = json.load(f)["open_shell"]["sizes"]
+    st = synthetic.Structure(**sizes)
+    for k, v in over.items():
+        setattr(st, k, v)
+    return st
+
+
+def test_open_shell_fock_route():
+    """computeF_RO_CPU (utils.py:97-169), computeLagrange, computeE_elec with
+    both HighSpin settings, and ENERGY1r's no1 > 0, MSpin != 0 route; the
+    in-place zeroing of the cj12 / ck12 diagonals from no1 on."""
+    g = load_golden("open_shell")
+    p = open_shell_param()
+    cj, ck = g["cj12"].copy(), g["ck12"].copy()
+    F = orc.fock_ro(g["J_ri"], g["K_ri"], g["n"], g["H"], cj, ck, p)
+    assert nrel(F, g["F_ro"]) < TOL
+    assert np.array_equal(cj, g["cj12_zeroed"]) and np.array_equal(ck, g["ck12_zeroed"])
+    elag = orc.lagrange(F, g["C"], p)
+    assert nrel(elag, g["elag_F"]) < TOL
+    assert abs(orc.e_elec(g["H"], g["C"], g["n"], elag, p) - float(g["E_F"])) < TOL * abs(float(g["E_F"]))
+    ph = open_shell_param(HighSpin=True)
+    Eh = orc.e_elec(g["H"], g["C"], g["n"], elag, ph)
+    assert abs(Eh - float(g["E_F_highspin"])) < TOL * abs(Eh)
+    E, el1, sd, md = orc.energy1r(g["C"], g["n"], g["H"], None, g["b"], g["cj12"].copy(), g["ck12"].copy(), p)
+    assert abs(E - float(g["E1r"])) < TOL * abs(E)
+    assert nrel(el1, g["elag1r"]) < TOL
