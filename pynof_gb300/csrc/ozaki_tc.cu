@@ -203,6 +203,37 @@ __device__ __forceinline__ long long split_round(float t, int frac, float two_fr
   return (long long)((unsigned long long)(long long)ti << frac) + fi;
 }
 
+// Drain of the exact groups g = 2..gE of CW columns of this warp's TMEM lanes
+// into R: group g holds FP32 integer multiples of 2^-7g below 2^22 units, taken
+// out with magic_int and combined as sum_g i_g 2^(7 (gE - g)) (units of
+// 2^-7gE; groups 3 and 4 fit one int32, < 2^30), scaled by 2^fr.
+template <int BN, int gE, int CW>
+__device__ __forceinline__ void drain_exact(uint32_t lbase, long long (&R)[CW], int fr) {
+#pragma unroll
+  for (int h = 0; h < CW / 4; ++h) {
+    uint32_t v2[4], v3[4], v4[4];
+    tmem_ld4_async(lbase + (uint32_t)(h * 4), v2);
+    if (gE >= 3) tmem_ld4_async(lbase + (uint32_t)(BN + h * 4), v3);
+    if (gE >= 4) tmem_ld4_async(lbase + (uint32_t)(2 * BN + h * 4), v4);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i2 = magic_int(__uint_as_float(v2[j]), 16384.0f);  // 2^14
+      long long acc;
+      if (gE == 2) {
+        acc = i2;
+      } else if (gE == 3) {
+        acc = (long long)i2 * 128 + magic_int(__uint_as_float(v3[j]), 2097152.0f);  // 2^21
+      } else {
+        const int i34 = magic_int(__uint_as_float(v3[j]), 2097152.0f) * 128 +
+                        magic_int(__uint_as_float(v4[j]), 268435456.0f);  // 2^28
+        acc = (long long)i2 * 16384 + i34;
+      }
+      R[h * 4 + j] += (long long)((unsigned long long)acc << fr);
+    }
+  }
+}
+
 // int64 fixed point z * 2^scale -> double, round to nearest even, integer ops
 // only (the FP64 pipe is narrow on this part).  The leading one is moved to
 // bit 63; the top 53 bits are the significand (implicit bit included, so adding
@@ -245,35 +276,76 @@ struct KArgs {
   int withhold;
 };
 
-// MMAs of one stage, fully unrolled for S slices: a product (s, t) reads slice
-// tile s of A and t of B, whose descriptors differ from the stage's first tile
-// descriptors only in the start-address field.
-template <int S, int BN>
-__device__ __forceinline__ void issue_inexact(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool& started) {
-  using T = TileCfg<BN, 0>;
-#pragma unroll
-  for (int s = 1; s <= S; ++s)
-#pragma unroll
-    for (int t = 1; t <= S + 1 - s; ++t) {
-      if (s + t <= 4) continue;
-      mma_bf16(tmem + 3 * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)), db + (uint64_t)((t - 1) * (T::B_TILE >> 4)),
-               idesc, started);
-      started = true;
-    }
+// bf16 MMA with an A-collector qualifier: COLL 0 none, 1 fill (read A from
+// shared memory and keep it in the tensor core's collector), 2 use (take A
+// from the collector), 3 lastuse (take it and release the collector).
+template <int COLL>
+__device__ __forceinline__ void mma_bf16_c(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate) {
+  if constexpr (COLL == 0)
+    mma_bf16(d_tmem, a, b, idesc, accumulate);
+  else if constexpr (COLL == 1)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate)
+        : "memory");
+  else if constexpr (COLL == 2)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate)
+        : "memory");
 }
 
-template <int S, int BN>
-__device__ __forceinline__ void issue_exact(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool first) {
+// Products of one stage (S digit slices; product (s, t) of A slice s and B
+// slice t goes to group g = s + t, kept only for g <= S + 1), fully unrolled
+// and ordered by A slice: the products of one A slice run back to back and
+// take A from the collector after the first, so each A slice tile is read
+// from shared memory once per stage (6 reads instead of 21 at S = 6; B is
+// read per product).  The slice tiles' descriptors differ from the stage's
+// first ones only in the start-address field.
+//   SEL 0: every product; 1: the FP32 group only (g >= 5); 2: the exact
+//   groups only (g <= 4, accumulator columns (g - 2) BN).
+//   restart_exact: the exact groups start from zero (their first product,
+//   s = 1, overwrites); restart_f: the FP32 group (at 3 BN) starts from zero.
+template <int S, int BN, int SEL>
+__device__ __forceinline__ void issue_products(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc,
+                                               bool restart_exact, bool restart_f) {
   using T = TileCfg<BN, 0>;
-  constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
+  bool f_first = true;
 #pragma unroll
-  for (int gg = 2; gg <= gE; ++gg) {
+  for (int s = 1; s <= S; ++s) {
+    const uint64_t das = da + (uint64_t)((s - 1) * (TILE_BYTES >> 4));
+    // this slice's products under SEL: t in [t0, t1]
+    const int t0 = SEL == 1 ? (5 - s > 1 ? 5 - s : 1) : 1;
+    const int t1 = SEL == 2 ? (4 - s < S + 1 - s ? 4 - s : S + 1 - s) : S + 1 - s;
 #pragma unroll
-    for (int s = 1; s < gg; ++s) {
-      const int t = gg - s;
-      if (s > S || t > S) continue;
-      mma_bf16(tmem + (gg - 2) * BN, da + (uint64_t)((s - 1) * (TILE_BYTES >> 4)),
-               db + (uint64_t)((t - 1) * (T::B_TILE >> 4)), idesc, !(first && s == 1));
+    for (int t = t0; t <= t1; ++t) {
+      const int gg = s + t;
+      const bool exact = gg <= 4;
+      const uint32_t d = tmem + (uint32_t)((exact ? gg - 2 : 3) * BN);
+      const uint64_t dbt = db + (uint64_t)((t - 1) * (T::B_TILE >> 4));
+      bool acc;
+      if (exact) {
+        acc = !(restart_exact && s == 1);
+      } else {
+        acc = !(restart_f && f_first);
+        f_first = false;
+      }
+      if (t0 == t1)
+        mma_bf16_c<0>(d, das, dbt, idesc, acc);
+      else if (t == t0)
+        mma_bf16_c<1>(d, das, dbt, idesc, acc);
+      else if (t == t1)
+        mma_bf16_c<3>(d, das, dbt, idesc, acc);
+      else
+        mma_bf16_c<2>(d, das, dbt, idesc, acc);
     }
   }
 }
@@ -453,28 +525,29 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
         }
         const int c = kb / CH;
         const bool first = (kb % CH) == 0;
-        if (g.fdrain) {
-          // the FP32 accumulator is drained with the exact groups: restart it every chunk
-          if (first && c > 0) {
-            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
-              signal_abort(abort_flag);
-              break;
-            }
-            tc_fence_after();
+        if (!first) {
+          issue_products<S, BN, 0>(tmem, da, db, idesc, false, false);
+        } else if (c == 0) {
+          issue_products<S, BN, 0>(tmem, da, db, idesc, true, true);
+        } else if (g.fdrain) {
+          // the FP32 accumulator is drained with the exact groups: it restarts
+          // every chunk, after the drain
+          if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
+            signal_abort(abort_flag);
+            break;
           }
-          if (first) f_started = false;
-          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
+          tc_fence_after();
+          issue_products<S, BN, 0>(tmem, da, db, idesc, true, true);
         } else {
-          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
-          if (first && c > 0) {
-            if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
-              signal_abort(abort_flag);
-              break;
-            }
-            tc_fence_after();
+          // the FP32 group runs ahead while the exact groups drain
+          issue_products<S, BN, 1>(tmem, da, db, idesc, false, false);
+          if (!mbar_wait(accempty_bar, (c - 1) & 1, abort_flag, a.wait_ns)) {
+            signal_abort(abort_flag);
+            break;
           }
+          tc_fence_after();
+          issue_products<S, BN, 2>(tmem, da, db, idesc, true, false);
         }
-        issue_exact<S, BN>(tmem, da, db, idesc, first);
         if ((kb % CH) == CH - 1 || kb == nkb - 1) mma_commit(accfull_bar);
         mma_commit(empty_bar(st));
       }
@@ -565,31 +638,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       }
       tc_fence_after();
       const int fr = g.fdrain ? a.frac : 0;  // fraction bits carried by R from the start
-#pragma unroll
-      for (int h = 0; h < (cols_live ? CW / 4 : 0); ++h) {
-        // the exact groups' integers (|.| < 2^22 each), combined as
-        // sum_g i_g 2^(7 (gE - g)): groups 3 and 4 fit one int32 (< 2^30)
-        uint32_t v2[4], v3[4], v4[4];
-        tmem_ld4_async(lbase + (uint32_t)(h * 4), v2);
-        if (gE >= 3) tmem_ld4_async(lbase + (uint32_t)(BN + h * 4), v3);
-        if (gE >= 4) tmem_ld4_async(lbase + (uint32_t)(2 * BN + h * 4), v4);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int i2 = magic_int(__uint_as_float(v2[j]), 16384.0f);  // 2^14
-          long long acc;
-          if (gE == 2) {
-            acc = i2;
-          } else if (gE == 3) {
-            acc = (long long)i2 * 128 + magic_int(__uint_as_float(v3[j]), 2097152.0f);  // 2^21
-          } else {
-            const int i34 = magic_int(__uint_as_float(v3[j]), 2097152.0f) * 128 +
-                            magic_int(__uint_as_float(v4[j]), 268435456.0f);  // 2^28
-            acc = (long long)i2 * 16384 + i34;
-          }
-          R[h * 4 + j] += (long long)((unsigned long long)acc << fr);
-        }
-      }
+      if (cols_live) drain_exact<BN, gE, CW>(lbase, R, fr);
       if (has_inexact && g.fdrain && cols_live) {
 #pragma unroll
         for (int h = 0; h < CW / 8; ++h) {
@@ -608,6 +657,7 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
       const bool got = mbar_wait(done_bar, 0, abort_flag, a.wait_ns);
       if (!__all_sync(0xffffffffu, got)) signal_abort(abort_flag);
     }
+
     // CTA-uniform go / no-go for the assembly (every epilogue warp arrives here)
     if (epi_barrier_any(*abort_flag != 0)) ok = false;
     if (ok) {
@@ -892,7 +942,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         const int n_valid = min(BN, g.N - n0);
         const int n_mma = (n_valid + 15) & ~15;
         const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
-        bool f_started = false;
         for (int kb = 0; kb < nkb; ++kb) {
           const int st = gkb % STAGES;
           if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag, a.wait_ns)) {
@@ -905,6 +954,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           const uint64_t da = desc_tile(sa, BM), db = desc_tile(sa + a_bytes, BN);
           const int c = kb / CH;
           const bool first = (kb % CH) == 0;
+          const bool chunk_last = (kb % CH) == CH - 1 || kb == nkb - 1;
           // a new tile (or, with fdrain, every chunk) must wait until the
           // epilogue has taken everything out of TMEM; inside a tile the FP32
           // group may run ahead while the exact groups drain
@@ -916,22 +966,26 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
             }
             tc_fence_after();
           }
-          if (g.fdrain && first) f_started = false;
-          if (has_inexact) issue_inexact<S, BN>(tmem, da, db, idesc, f_started);
-          if (!g.fdrain && first && c > 0) {
+          if (first && c > 0 && !g.fdrain) {
+            // the FP32 group runs ahead while the exact groups drain
+            issue_products<S, BN, 1>(tmem, da, db, idesc, false, false);
             if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a.wait_ns)) {
               signal_abort(abort_flag);
               aborted = true;
               break;
             }
             tc_fence_after();
+            issue_products<S, BN, 2>(tmem, da, db, idesc, true, false);
+          } else {
+            // the tile's first stage restarts every accumulator (with fdrain,
+            // every chunk's first stage does)
+            issue_products<S, BN, 0>(tmem, da, db, idesc, first, first && (c == 0 || g.fdrain));
           }
-          issue_exact<S, BN>(tmem, da, db, idesc, first);
-          if ((kb % CH) == CH - 1 || kb == nkb - 1) {
+          mma_commit(empty_bar(st));
+          if (chunk_last) {
             mma_commit(accfull_bar);
             ++gch;
           }
-          mma_commit(empty_bar(st));
           ++gkb;
         }
       }
@@ -1011,29 +1065,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         }
         tc_fence_after();
         const int fr = g.fdrain ? a.frac : 0;
-#pragma unroll
-        for (int h = 0; h < (cols_live ? CW / 4 : 0); ++h) {
-          uint32_t v2[4], v3[4], v4[4];
-          tmem_ld4_async(lbase + (uint32_t)(h * 4), v2);
-          if (gE >= 3) tmem_ld4_async(lbase + (uint32_t)(BN + h * 4), v3);
-          if (gE >= 4) tmem_ld4_async(lbase + (uint32_t)(2 * BN + h * 4), v4);
-          tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int i2 = magic_int(__uint_as_float(v2[j]), 16384.0f);
-            long long acc;
-            if (gE == 2) {
-              acc = i2;
-            } else if (gE == 3) {
-              acc = (long long)i2 * 128 + magic_int(__uint_as_float(v3[j]), 2097152.0f);
-            } else {
-              const int i34 = magic_int(__uint_as_float(v3[j]), 2097152.0f) * 128 +
-                              magic_int(__uint_as_float(v4[j]), 268435456.0f);
-              acc = (long long)i2 * 16384 + i34;
-            }
-            R[h * 4 + j] += (long long)((unsigned long long)acc << fr);
-          }
-        }
+        if (cols_live) drain_exact<BN, gE, CW>(lbase, R, fr);
         const bool last = c == nchunks - 1;
         if (has_inexact && cols_live && (g.fdrain || last)) {
           // the FP32 group: drained every chunk (fdrain) or folded in at the end
