@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
-    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision"], default="jk",
+    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision", "mo"], default="jk",
                     help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream; "
-                         "precision: every split form against FP64 (J, K, E, orbital gradient)")
+                         "precision: every split form against FP64 (J, K, E, orbital gradient); "
+                         "mo: computeJKH_MO and computeLagrange2 per kernel, with the bandwidth kernels' GB/s")
     ap.add_argument("--nmol", type=int, default=64)
     ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rate", type=float, default=10.0)
@@ -675,6 +676,97 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def mo_kernel_bytes(N, P, Q, S):
+    """Algorithmic DRAM bytes per call of each bandwidth-bound kernel of
+    computeJKH_MO ("jkh") and computeLagrange2 ("lag2"): every input read once
+    and every output written once (float64 = 8 B; a digit slicing reads 8 B and
+    writes 2S B per element, its exponent pass reads the 8 B once more)."""
+    dig = 8 + 2 * S
+    jkh = {
+        "slice_digits": (P * N + P * N * Q) * dig,
+        "slice_rowexp": (P * N + P * N * Q) * 8,
+        "gather_diag": 16 * P * Q,
+        "row_sumsq": 8 * P * P * Q + 8 * P * P,
+        "col_dot": 16 * N * P + 8 * P,
+    }
+    lag2 = {
+        "slice_digits": (N * N + P * N * Q + N * P * Q + P * P * Q) * dig,
+        "slice_rowexp": (N * N + P * N * Q + N * P * Q + P * P * Q) * 8,
+        "gather_diag": 16 * P * Q,
+        "copy_zero_diag": 16 * P * P,
+        "add_scaled_rows": 24 * P * Q,
+        "make_exchange_operand": 16 * P * P * Q + 8 * P * P,
+        "lagrange2_hterm": 16 * N * N + 8 * N * P,
+    }
+    fused = dict(lag2)
+    fused["row_sumsq"] = 8 * P * P * Q + 8 * P * P
+    fused["col_dot"] = 16 * N * P + 8 * P
+    return {"jkh": jkh, "lag2": lag2, "fused": fused}
+
+
+def run_mo(args):
+    """computeJKH_MO, computeLagrange2 and the two in one call (what each
+    orbital step of the solver makes) on the split-product path at one
+    workload: calls/s and, per kernel, ms per call; for the bandwidth-bound
+    kernels their algorithmic bytes and GB/s against the measured HBM copy
+    rate.  Times come from the library's event profiler (CUDA events on the
+    launch stream) over --steps calls after --warmup."""
+    import torch
+
+    from pynof_gb300 import _lib, integrals, nof, ops
+
+    torch.cuda.set_device(0)
+    st, b, C, H, n = make_workload(args.workload)
+    N, P, Q, S = st.nbf, st.nbf5, st.nbfaux, args.nslices
+    db, dC, dH, dn = ops.to_device(b), ops.to_device(C), ops.to_device(H), ops.to_device(n)
+    integrals.set_precision("mixed", S)
+    prep = integrals.prepared(db, S)
+    cj, ck = nof.cjckd8(n, st)
+    np.fill_diagonal(cj, 0.0)
+    np.fill_diagonal(ck, 0.0)
+    dcj, dck = ops.to_device(cj), ops.to_device(ck)
+    calls = {
+        "jkh": lambda: ops.jkh_mo_ri_mixed(dC, dH, prep, P),
+        "lag2": lambda: ops.lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta, st.nalpha),
+        "fused": lambda: ops.jkh_lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta, st.nalpha),
+    }
+    peaks, peak_src = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    nbytes = mo_kernel_bytes(N, P, Q, S)
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, fn in calls.items():
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        _lib.profile_start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        prof = _lib.profile_stop()
+        ops.check_device_status()
+        ms = e0.elapsed_time(e1) / args.steps
+        kern = {}
+        for k, (launches, total) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+            rec = {"launches_per_call": launches / args.steps, "ms_per_call": total / args.steps,
+                   "share": total / args.steps / ms}
+            if k in nbytes[name]:
+                gbs = nbytes[name][k] / (total / args.steps * 1e-3) / 1e9
+                rec.update({"bytes_per_call": nbytes[name][k], "gbs": gbs, "frac_of_hbm": gbs / hbm})
+            kern[k] = rec
+        out[name] = {"calls_per_s": 1e3 / ms, "ms_per_call": ms, "kernels": kern}
+    line = {"mode": "mo", "metric": "computeJKH_MO and computeLagrange2 calls/s (split products, nslices=%d)" % S,
+            "unit": "calls/s", "data": "synthetic",
+            "config": {"workload": f"nbf={N} naux={Q} nbf5={P}", "steps": args.steps, "warmup": args.warmup},
+            "hbm_peak_gbs": hbm, "peak_source": f"hbm_gbs of {peak_src} MEASURED_PEAKS.json",
+            "computeJKH_MO": out["jkh"], "computeLagrange2": out["lag2"],
+            "computeJKH_MO+computeLagrange2 (one call)": out["fused"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -685,6 +777,8 @@ def main():
         run_serve(args)
     elif args.mode == "precision":
         run_precision(args)
+    elif args.mode == "mo":
+        run_mo(args)
     else:
         run_ours(args)
 

@@ -359,6 +359,21 @@ int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, co
                           const double* ck12, int nbf, int nbf5, int naux, int nbeta, int nalpha, int nslices,
                           double* elag, double* Hmat, void* workspace, size_t workspace_bytes, void* stream);
 
+/* A3 + A5  computeJKH_MO and computeLagrange2 at the same orbitals in one call
+ *     on the tensor cores: the outputs of gb_jkh_mo_ri_mixed and
+ *     gb_lagrange2_ri_mixed.  The orbital optimiser evaluates both at every
+ *     step (energy from J_MO, K_MO, H_core; gradient from elag: calcorbe /
+ *     calcorbg, pynof/pnof.py:1103-1131, in orbopt_adam, pynof/minimization.py:
+ *     200-253); one half transform and one MO transform bMO[a][q][l] = (aq|l)
+ *     serve both, since J_MO = d d^T with d[p] = (pp|l) and
+ *     K_MO[p][q] = sum_l (pq|l)^2 come from its first nbf5 rows.  Same
+ *     workspace as gb_lagrange2_ri_mixed. */
+size_t gb_jkh_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);
+int gb_jkh_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n,
+                              const double* cj12, const double* ck12, int nbf, int nbf5, int naux, int nbeta,
+                              int nalpha, int nslices, double* J_MO, double* K_MO, double* H_core, double* elag,
+                              double* Hmat, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched A1 (many molecules of different sizes) on the tensor cores.  No
  * counterpart in the reference, which builds one molecule per call.  The half

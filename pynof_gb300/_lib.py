@@ -95,6 +95,9 @@ SIGNATURES = {
     "gb_jkh_mo_ri_mixed": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _Z, _P]),
     "gb_lagrange2_ri_workspace_mixed": (_Z, [_I, _I, _I, _I]),
     "gb_lagrange2_ri_mixed": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
+    "gb_jkh_lagrange2_ri_workspace_mixed": (_Z, [_I, _I, _I, _I]),
+    "gb_jkh_lagrange2_ri_mixed": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _Z,
+                                       _P]),
 }
 
 _lock = threading.Lock()

@@ -140,6 +140,44 @@ __global__ void lagrange2_finish_kernel(const double* __restrict__ bMO, const do
   }
 }
 
+// Exchange operand of the tensor-core Lagrangian: Y[b][q][k] = ck12[b][q]
+// bMO[b][q][k] for q != b and -w[b][k] on the diagonal block q == b, so that
+// -sum_(q,k) bMO[a][q][k] Y[b][q][k] also carries + sum_k bMO[a][b][k] w[b][k].
+// Grid-stride over (b, q) rows of Q; two elements per thread and step
+// (16-byte accesses when Q is even).
+__global__ void make_exchange_operand_kernel(const double* __restrict__ bMO, const double* __restrict__ ck12,
+                                             const double* __restrict__ w, double* __restrict__ Y, int P, int Q) {
+  const long long rows = (long long)P * P;
+  const int half = Q >> 1;
+  const bool even = (Q & 1) == 0;
+  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int b = (int)(row / P), q = (int)(row % P);
+    const bool diag = q == b;
+    const double c = diag ? -1.0 : ck12[(long long)b * P + q];
+    const double* src = diag ? w + (long long)b * Q : bMO + row * Q;
+    double* dst = Y + row * Q;
+    if (even) {
+      for (int k2 = threadIdx.x; k2 < half; k2 += blockDim.x) {
+        const double2 v = __ldcs(reinterpret_cast<const double2*>(src) + k2);
+        __stcs(reinterpret_cast<double2*>(dst) + k2, make_double2(c * v.x, c * v.y));
+      }
+    } else {
+      for (int k = threadIdx.x; k < Q; k += blockDim.x) dst[k] = c * src[k];
+    }
+  }
+}
+
+// elag[a][b] += n[b] Hmat[a][b] for b < P; elag[a][b] = 0 for b >= P
+__global__ void lagrange2_hterm_kernel(const double* __restrict__ Hmat, const double* __restrict__ n,
+                                       double* __restrict__ elag, int N, int P) {
+  const long long total = (long long)N * N;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(i / N), b = (int)(i % N);
+    elag[i] = b < P ? elag[i] + n[b] * Hmat[(long long)a * P + b] : 0.0;
+  }
+}
+
 __global__ void zero_tail_cols_kernel(double* __restrict__ elag, int N, int P) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int W = N - P;
@@ -196,6 +234,24 @@ int launch_add_scaled_rows(double* w, const double* d, const double* n, int P, i
 
 int launch_make_ck_weighted(const double* bMO, const double* ck12, double* Y, int P, int Q, cudaStream_t s) {
   GB_LAUNCH("make_ck_weighted", s, make_ck_weighted_kernel<<<dim3(cdiv(Q, 128), P, P), 128, 0, s>>>(bMO, ck12, Y, P, Q));
+  return GB_OK;
+}
+
+int launch_make_exchange_operand(const double* bMO, const double* ck12, const double* w, double* Y, int P, int Q,
+                                 cudaStream_t s) {
+  const long long rows = (long long)P * P;
+  if (rows == 0 || Q == 0) return GB_OK;
+  const unsigned grid = (unsigned)(rows < 152LL * 16 ? rows : 152LL * 16);
+  GB_LAUNCH("make_exchange_operand", s,
+            make_exchange_operand_kernel<<<grid, 256, 0, s>>>(bMO, ck12, w, Y, P, Q));
+  return GB_OK;
+}
+
+int launch_lagrange2_hterm(const double* Hmat, const double* n, double* elag, int N, int P, cudaStream_t s) {
+  const long long total = (long long)N * N;
+  if (total == 0) return GB_OK;
+  const unsigned grid = (unsigned)(cdiv(total, 256) < 152u * 8 ? cdiv(total, 256) : 152u * 8);
+  GB_LAUNCH("lagrange2_hterm", s, lagrange2_hterm_kernel<<<grid, 256, 0, s>>>(Hmat, n, elag, N, P));
   return GB_OK;
 }
 

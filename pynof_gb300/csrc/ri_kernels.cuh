@@ -25,6 +25,12 @@ int launch_add_scaled_rows(double* w, const double* d, const double* n, int P, i
                            cudaStream_t s);
 // Y[b][q][k] = (q != b) ck12[b][q] bMO[b][q][k]
 int launch_make_ck_weighted(const double* bMO, const double* ck12, double* Y, int P, int Q, cudaStream_t s);
+// Y[b][q][k] = ck12[b][q] bMO[b][q][k] (q != b), -w[b][k] (q == b): the exchange
+// operand of the tensor-core Lagrangian with the w term folded into its diagonal block
+int launch_make_exchange_operand(const double* bMO, const double* ck12, const double* w, double* Y, int P, int Q,
+                                 cudaStream_t s);
+// elag[a][b] += n[b] Hmat[a][b] (b < P); elag[a][b] = 0 (b >= P)
+int launch_lagrange2_hterm(const double* Hmat, const double* n, double* elag, int N, int P, cudaStream_t s);
 // elag[a][b] += n[b] Hmat[a][b] + sum_k bMO[a][b][k] w[b][k] (b < P); elag[a][b] = 0 (b >= P)
 int launch_lagrange2_finish(const double* bMO, const double* w, const double* Hmat, const double* n,
                             double* elag, int N, int P, int Q, cudaStream_t s);

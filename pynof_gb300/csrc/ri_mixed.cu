@@ -446,27 +446,21 @@ extern "C" size_t gb_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, i
   return c.used;
 }
 
-extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n,
-                                     const double* cj12, const double* ck12, int nbf, int nbf5, int naux, int nbeta,
-                                     int nalpha, int nslices, double* elag, double* Hmat, void* workspace,
-                                     size_t workspace_bytes, void* stream) {
-  clear_error();
-  const int N = nbf, P = nbf5, Q = naux, S = nslices;
-  GB_TRY(check_mixed(N, P, Q, S));
-  GB_REQUIRE((long long)P * Q < 2147483647LL, GB_ERR_BAD_SHAPE, "gb_lagrange2_ri_mixed: nbf5*naux too large");
-  GB_REQUIRE(0 <= nbeta && nbeta <= nalpha && nalpha <= P, GB_ERR_BAD_SHAPE,
-             "gb_lagrange2_ri_mixed: need 0 <= nbeta <= nalpha <= nbf5");
-  GB_REQUIRE(C && H && prep && n && cj12 && ck12 && elag && Hmat, GB_ERR_INVALID_ARG,
-             "gb_lagrange2_ri_mixed: null pointer");
-  GB_REQUIRE(workspace_bytes >= gb_lagrange2_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
-             "gb_lagrange2_ri_mixed: workspace too small");
+namespace {
+// computeLagrange2 on the tensor cores; with J_MO, K_MO, H_core non-null also
+// computeJKH_MO at the same orbitals, from the same transform: bMO[a][q][l] =
+// (aq|l), so d[p] = bMO[p][p], J_MO = d d^T and K_MO[p][q] = sum_l bMO[p][q][l]^2
+// (the first nbf5 rows of bMO), H_core[p] = C_p^T H C_p.
+int lagrange2_mixed_body(const double* C, const double* H, const void* prep, const double* n, const double* cj12,
+                         const double* ck12, int N, int P, int Q, int nbeta, int nalpha, int S, double* elag,
+                         double* Hmat, double* J_MO, double* K_MO, double* H_core, void* workspace,
+                         size_t workspace_bytes, cudaStream_t s) {
   Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
   Prepared pr;
   prepared_layout(pc, N, Q, S, &pr);
   Carve wc(workspace, workspace_bytes);
   Lag2MixedWs w;
   lag2_mixed_layout(wc, N, P, Q, S, &w);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // C^T sliced once for all nbf rows; its first nbf5 rows are the half transform's A
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Aall, s));
@@ -480,8 +474,20 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   gm.C = w.bMO; gm.c_sb = Q; gm.c_r = lin((long long)P * Q); gm.c_c = lin(1);
   gm.sym = SYM_NONE; gm.tag = "ozaki_tc:bMO"; gm.tile_counter = w.ctr;
   GB_TRY(ozaki_gemm(w.Aall, w.Tt, gm, s));
-  GB_TRY(hcore_f64(C, H, N, P, w.X, nullptr, Hmat, s));
+  GB_TRY(hcore_f64(C, H, N, P, w.X, H_core, Hmat, s));
   GB_TRY(launch_gather_diag(w.bMO, w.d, P, Q, (long long)P * Q + Q, s));
+  if (J_MO) {
+    GemmF64 gj{};
+    gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1;
+    gj.A = {w.d, 0, lin(Q), lin(1)};
+    gj.B = {w.d, 0, lin(1), lin(Q)};
+    gj.C = {J_MO, 0, lin(P), lin(1)};
+    gj.alpha = 1.0; gj.beta = 0.0; gj.sym = SYM_ROWCOL;
+    gj.a_kfast = true; gj.b_kfast = true;
+    gj.tag = "gemm_f64:small";
+    GB_TRY(gemm_f64(gj, s));
+    GB_TRY(launch_row_sumsq(w.bMO, K_MO, (long long)P * P, Q, s));
+  }
   GB_TRY(launch_copy_zero_diag(cj12, w.cjm, P, s));
   GemmF64 gw{};
   gw.M = P; gw.N = Q; gw.K = P; gw.batch = 1;
@@ -493,7 +499,8 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
   gw.tag = "gemm_f64:small";
   GB_TRY(gemm_f64(gw, s));
   GB_TRY(launch_add_scaled_rows(w.w, w.d, n, P, Q, nbeta, nalpha, s));
-  GB_TRY(launch_make_ck_weighted(w.bMO, ck12, w.Y, P, Q, s));
+  // the w term rides in the diagonal blocks of the exchange operand
+  GB_TRY(launch_make_exchange_operand(w.bMO, ck12, w.w, w.Y, P, Q, s));
   // elag[a][b] = -sum_(q,l) bMO[a][(q,l)] Y[b][(q,l)], K cut into w.ns equal
   // ranges (split s = batch s: element (row, k) at row * P Q + s kc + k)
   GB_TRY(slice_operand(SliceSrc{w.bMO, w.kc, lin((long long)P * Q), lin(1), true}, w.Sx, s));
@@ -510,5 +517,49 @@ extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const voi
     ge.C = elag; ge.c_sb = 0; ge.c_r = lin(N); ge.c_c = lin(1);
     GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
   }
-  return launch_lagrange2_finish(w.bMO, w.w, Hmat, n, elag, N, P, Q, s);
+  return launch_lagrange2_hterm(Hmat, n, elag, N, P, s);
+}
+
+int check_lagrange2_mixed(int N, int P, int Q, int nbeta, int nalpha, int S, const char* who) {
+  GB_TRY(check_mixed(N, P, Q, S));
+  GB_REQUIRE((long long)P * Q < 2147483647LL, GB_ERR_BAD_SHAPE, "%s: nbf5*naux too large", who);
+  GB_REQUIRE(0 <= nbeta && nbeta <= nalpha && nalpha <= P, GB_ERR_BAD_SHAPE, "%s: need 0 <= nbeta <= nalpha <= nbf5",
+             who);
+  return GB_OK;
+}
+}  // namespace
+
+extern "C" int gb_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n,
+                                     const double* cj12, const double* ck12, int nbf, int nbf5, int naux, int nbeta,
+                                     int nalpha, int nslices, double* elag, double* Hmat, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(check_lagrange2_mixed(N, P, Q, nbeta, nalpha, S, "gb_lagrange2_ri_mixed"));
+  GB_REQUIRE(C && H && prep && n && cj12 && ck12 && elag && Hmat, GB_ERR_INVALID_ARG,
+             "gb_lagrange2_ri_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_lagrange2_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "gb_lagrange2_ri_mixed: workspace too small");
+  return lagrange2_mixed_body(C, H, prep, n, cj12, ck12, N, P, Q, nbeta, nalpha, S, elag, Hmat, nullptr, nullptr,
+                              nullptr, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" size_t gb_jkh_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices) {
+  return gb_lagrange2_ri_workspace_mixed(nbf, nbf5, naux, nslices);
+}
+
+extern "C" int gb_jkh_lagrange2_ri_mixed(const double* C, const double* H, const void* prep, const double* n,
+                                         const double* cj12, const double* ck12, int nbf, int nbf5, int naux,
+                                         int nbeta, int nalpha, int nslices, double* J_MO, double* K_MO,
+                                         double* H_core, double* elag, double* Hmat, void* workspace,
+                                         size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(check_lagrange2_mixed(N, P, Q, nbeta, nalpha, S, "gb_jkh_lagrange2_ri_mixed"));
+  GB_REQUIRE(C && H && prep && n && cj12 && ck12 && J_MO && K_MO && H_core && elag && Hmat, GB_ERR_INVALID_ARG,
+             "gb_jkh_lagrange2_ri_mixed: null pointer");
+  GB_REQUIRE(workspace_bytes >= gb_jkh_lagrange2_ri_workspace_mixed(N, P, Q, S), GB_ERR_WORKSPACE,
+             "gb_jkh_lagrange2_ri_mixed: workspace too small");
+  return lagrange2_mixed_body(C, H, prep, n, cj12, ck12, N, P, Q, nbeta, nalpha, S, elag, Hmat, J_MO, K_MO, H_core,
+                              workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
 }

@@ -570,3 +570,22 @@ def lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: 
     _lib.call("gb_lagrange2_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), _ptr(n), _ptr(cj12), _ptr(ck12), N,
               nbf5, Q, nbeta, nalpha, S, _ptr(elag), _ptr(Hmat), wp, wn, _stream(dev))
     return elag, Hmat
+
+
+def jkh_lagrange2_ri_mixed(C, H, prep: PreparedRI, n, cj12, ck12, nbf5: int, nbeta: int, nalpha: int, out=None):
+    """computeJKH_MO and computeLagrange2 at the same orbitals in one call on
+    the tensor cores (one half transform and one MO transform serve both):
+    (J_MO, K_MO, H_core, elag, Hmat)."""
+    N, Q, S = prep.nbf, prep.naux, prep.nslices
+    _require(C, (N, N), "C")
+    _require(H, (N, N), "H")
+    _require(n, (nbf5,), "n")
+    _require(cj12, (nbf5, nbf5), "cj12")
+    _require(ck12, (nbf5, nbf5), "ck12")
+    dev = prep.device
+    J_MO, K_MO, H_core, elag, Hmat = _outs(out, [(nbf5, nbf5), (nbf5, nbf5), (nbf5,), (N, N), (N, nbf5)], dev)
+    wp, wn = _ws("gb_jkh_lagrange2_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
+    _lib.call("gb_jkh_lagrange2_ri_mixed", _ptr(C), _ptr(H), prep.buf.data_ptr(), _ptr(n), _ptr(cj12), _ptr(ck12),
+              N, nbf5, Q, nbeta, nalpha, S, _ptr(J_MO), _ptr(K_MO), _ptr(H_core), _ptr(elag), _ptr(Hmat), wp, wn,
+              _stream(dev))
+    return J_MO, K_MO, H_core, elag, Hmat

@@ -121,9 +121,9 @@ class Backend:
         self.calls["lagrange2"] += 1
         mo_out, l2_out = (b["J"], b["K"], b["Hc"]), (b["elag"], b["Hmat"])
         if self.precision == "mixed":
-            ops.jkh_mo_ri_mixed(b["C"], self.H, self.prep, st.nbf5, out=mo_out)
-            ops.lagrange2_ri_mixed(b["C"], self.H, self.prep, b["n"], b["cj"], b["ck"], st.nbf5, st.nbeta,
-                                   st.nalpha, out=l2_out)
+            # one call: the half transform and the MO transform serve both
+            ops.jkh_lagrange2_ri_mixed(b["C"], self.H, self.prep, b["n"], b["cj"], b["ck"], st.nbf5, st.nbeta,
+                                       st.nalpha, out=mo_out + l2_out)
         else:
             ops.jkh_mo_ri(b["C"], self.H, self.b, st.nbf5, out=mo_out)
             ops.lagrange2_ri(b["C"], self.H, self.b, b["n"], b["cj"], b["ck"], st.nbf5, st.nbeta, st.nalpha,

@@ -144,6 +144,53 @@ def test_jkh_mo_and_lagrange2_mixed_vs_oracle(torch_cuda):
         assert nrel(c.cpu().numpy(), cr) < 1e-12 and nrel(Hm.cpu().numpy(), Hr) < 1e-12
 
 
+def test_jkh_lagrange2_fused_mixed(torch_cuda):
+    """computeJKH_MO and computeLagrange2 in one call (one half transform and
+    one MO transform for both) against the oracle, and against the two
+    separate calls on the same inputs."""
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import ops, synthetic
+
+    st = synthetic.Structure(nbf=130, nbfaux=520, ndoc=13, ncwo=4)
+    b, C, H, n = synthetic.make_inputs(st, 11)
+    P = st.nbf5
+    db, dC, dH = ops.to_device(b), ops.to_device(C), ops.to_device(H)
+    cj = 2 * np.outer(n, n)
+    ck = np.outer(n, n) + 0.1
+    ar, br, cr = orc.jkh_mo_ri(C, H, b, P)
+    elr, Hr = orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st)
+    dn, dcj, dck = ops.to_device(n), ops.to_device(cj), ops.to_device(ck)
+    for S, tol in ((6, 1e-10), (2, 1e-3)):
+        prep = ops.PreparedRI(db, nslices=S)
+        a, bb, c, el, Hm = ops.jkh_lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta, st.nalpha)
+        ops.check_device_status()
+        errs = [nrel(a.cpu().numpy(), ar), nrel(bb.cpu().numpy(), br), nrel(el.cpu().numpy(), elr)]
+        print(f"fused nslices={S}: J_MO {errs[0]:.2e} K_MO {errs[1]:.2e} elag {errs[2]:.2e}")
+        assert max(errs) < tol, (S, errs)
+        assert nrel(c.cpu().numpy(), cr) < 1e-12 and nrel(Hm.cpu().numpy(), Hr) < 1e-12
+        a2, b2, c2 = ops.jkh_mo_ri_mixed(dC, dH, prep, P)
+        el2, Hm2 = ops.lagrange2_ri_mixed(dC, dH, prep, dn, dcj, dck, P, st.nbeta, st.nalpha)
+        ops.check_device_status()
+        # the same FP64 assembly (H_core, Hmat) and the same Lagrangian code path
+        assert torch_cuda.equal(c, c2) and torch_cuda.equal(Hm, Hm2) and torch_cuda.equal(el, el2)
+        # J_MO, K_MO from a differently shaped transform: equal to the split precision
+        assert nrel(a.cpu().numpy(), a2.cpu().numpy()) < tol and nrel(bb.cpu().numpy(), b2.cpu().numpy()) < tol
+
+
+def test_jkh_lagrange2_fused_mixed_golden(case):
+    from pynof_gb300 import ops
+
+    g, p, d = case
+    prep = ops.PreparedRI(d["b"], nslices=6)
+    dH = ops.to_device(g["H"])
+    a, b, c, el, Hm = ops.jkh_lagrange2_ri_mixed(d["C"], dH, prep, ops.to_device(g["n_soft"]),
+                                                  ops.to_device(g["cj12"]), ops.to_device(g["ck12"]), p.nbf5,
+                                                  p.nbeta, p.nalpha)
+    ops.check_device_status()
+    for got, want in ((a, "J_MO_ri"), (b, "K_MO_ri"), (c, "H_core"), (el, "elag2_ri"), (Hm, "Hmat")):
+        assert nrel(got.cpu().numpy(), g[want]) < 1e-10, want
+
+
 @pytest.mark.parametrize("parts", [1, 2, 3, 7])
 def test_split_build_matches_one_call(torch_cuda, parts):
     """J and K formed in two C-ABI calls (J, then K over ranges of orbitals),

@@ -164,7 +164,14 @@ def test_c3_vs_oracle(c3, torch_cuda, form):
         mo = ops.jkh_mo_ri_mixed(d["C"], d["H"], prep, P)
         el, Hm = ops.lagrange2_ri_mixed(d["C"], d["H"], prep, d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)
         ops.check_device_status()
-        del prep
+        fused = [t.cpu().numpy() for t in
+                 ops.jkh_lagrange2_ri_mixed(d["C"], d["H"], prep, d["n"], d["cj"], d["ck"], P, st.nbeta, st.nalpha)]
+        ops.check_device_status()
+        ferr = {k: nrel(v, w) for k, v, w in zip(("J_MO", "K_MO", "H_core", "elag", "Hmat"), fused,
+                                                  list(ref["mo"]) + list(ref["l2"]))}
+        print("c3 fused computeJKH_MO + computeLagrange2: " + " ".join(f"{k} {v:.2e}" for k, v in ferr.items()))
+        assert all(v < TOL for v in ferr.values()), ferr
+        del prep, fused
         e_tol = E_TOL_MIXED
     Jh, Kh = J.cpu().numpy(), K.cpu().numpy()
     del J, K
