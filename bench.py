@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--maxit", type=int, default=200)
+    ap.add_argument("--time-limit", type=float, default=None, help="seconds per served solve (serve mode)")
     return ap.parse_args()
 
 
@@ -546,8 +547,9 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """A Poisson stream of full NOF solves, continuous batching, mixed path
-    (switching to FP64 near convergence) against the plain FP64 path."""
+    """A Poisson stream of full NOF solves, continuous batching: the mixed
+    path (six digit slices, closing Lagrangian on the FP64 path) against the
+    plain FP64 path, on the same requests."""
     import torch
 
     from pynof_gb300 import serve
@@ -557,7 +559,7 @@ def run_serve(args):
     out = {}
     for prec in ("mixed", "fp64"):
         srv = serve.Server(hbm_budget=150e9, slots=args.slots, precision=prec, nslices=args.nslices,
-                           fp64_switch=1e-2, tol=args.tol, maxit=args.maxit)
+                           tol=args.tol, maxit=args.maxit, final_fp64=True, time_limit=args.time_limit)
         out[prec] = srv.run(reqs)
         out[prec]["energies"] = {r.rid: r.E_elec for r in srv.results if r.converged}
     both = [k for k in out["fp64"]["energies"] if k in out["mixed"]["energies"]]
@@ -569,7 +571,9 @@ def run_serve(args):
             "config": {"requests": args.requests, "rate_per_s": args.rate,
                        "nbf": f"log-uniform {args.nbf_min}..{args.nbf_max}",
                        "naux": "4 nbf", "tol": args.tol, "maxit": args.maxit, "slots": args.slots,
-                       "hbm_budget_gb": 150, "fp64_switch_grad": 1e-2},
+                       "hbm_budget_gb": 150, "time_limit_per_solve_s": args.time_limit,
+                       "precision_switch": "six digit slices (FP64-class) throughout; closing Lagrangian "
+                                           "(reported energy) on the FP64 path"},
             "mixed": out["mixed"], "plain_fp64": out["fp64"],
             "max_abs_dE_mixed_vs_fp64_hartree": dE, "dE_over_requests_converged_in_both": len(both)}
     print(json.dumps(line), flush=True)

@@ -75,13 +75,27 @@ def reservation_bytes(st, precision: str, nslices: int) -> int:
 
 
 class Server:
+    """Continuous-batching NOF solve server.
+
+    precision "mixed": the split-product path (``nslices`` digits; six are
+    FP64-class, so by default no switch is made during the solve and only the
+    closing Lagrangian, i.e. the reported energy, is evaluated on the FP64
+    path, ``final_fp64``); ``fp64_switch`` or ``ladder`` (see
+    :func:`pynof_gb300.solver.solve`) switch precision up as the orbital
+    gradient falls.  precision "fp64": the plain DMMA path throughout.
+    ``time_limit`` bounds each solve (seconds of its own wall time)."""
+
     def __init__(self, hbm_budget: float = 150e9, slots: int = 8, precision: str = "mixed", nslices: int = 6,
-                 fp64_switch: float | None = 1e-2, tol: float = 1e-5, maxit: int = 200, device=None):
+                 fp64_switch: float | None = None, tol: float = 1e-5, maxit: int = 200, device=None,
+                 ladder=None, final_fp64: bool = True, time_limit: float | None = None):
         self.budget = int(hbm_budget)
         self.slots = slots
         self.precision = precision
         self.nslices = nslices
         self.fp64_switch = fp64_switch if precision == "mixed" else None
+        self.ladder = ladder if precision == "mixed" else None
+        self.final_fp64 = final_fp64 and precision == "mixed"
+        self.time_limit = time_limit
         self.tol = tol
         self.maxit = maxit
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -93,7 +107,12 @@ class Server:
         self.peak_active = 0
         self.results: list[Result] = []
         self.errors: list[tuple[int, str]] = []
+        self.steps = 0  # orbital steps (device Lagrangian evaluations) of finished solves
         self.solve_fn = self.solve_request
+
+    def _note_steps(self, k: int):
+        with self._lock:
+            self.steps += k
 
     def solve_request(self, req: Request):
         """Full NOF solve of one request on its own stream: (E, converged, iterations)."""
@@ -102,8 +121,10 @@ class Server:
         b, C, H, _ = synthetic.make_inputs(st, req.seed)
         be = solver.Backend(st, b, H, precision=self.precision, nslices=self.nslices, device=self.device)
         res = solver.solve(be, C, nof.gamma_guess_softmax(st), st, tol=self.tol, maxit=self.maxit,
-                           fp64_switch=self.fp64_switch)
+                           fp64_switch=self.fp64_switch, ladder=self.ladder, final_fp64=self.final_fp64,
+                           time_limit=self.time_limit)
         be.stream.synchronize()
+        self._note_steps(be.calls["lagrange2"])
         return res.E_elec, res.converged, res.iterations
 
     # ---- one solve -----------------------------------------------------
@@ -162,11 +183,17 @@ class Server:
             th.join()
         wall = time.perf_counter() - t0
         lat = np.array([r.latency for r in self.results]) if self.results else np.array([float("nan")])
+        conv = [r for r in self.results if r.converged]
+        clat = np.array([r.latency for r in conv]) if conv else np.array([float("nan")])
         return {
             "requests": len(requests), "completed": len(self.results), "failed": len(self.errors),
             "wall_s": wall, "solves_per_s": len(self.results) / wall,
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-            "converged": sum(r.converged for r in self.results),
+            "converged": len(conv), "converged_per_s": len(conv) / wall,
+            "p50_latency_converged_s": float(np.percentile(clat, 50)),
+            "p99_latency_converged_s": float(np.percentile(clat, 99)),
+            "orbital_steps_per_s": self.steps / wall,
             "peak_active": self.peak_active, "peak_reserved_gb": self.peak_reserved / 1e9,
             "precision": self.precision, "slots": self.slots, "budget_gb": self.budget / 1e9,
+            "time_limit_s": self.time_limit,
         }

@@ -233,8 +233,9 @@ def occoptr(gamma, C, be, p):
     return E, nit, success, gamma, n, cj12, ck12
 
 
-def orbopt_adam(gamma, C, be, p, state: SolveState):
-    """``minimization.py:200-253``: AMSgrad steps of orbital rotations."""
+def orbopt_adam(gamma, C, be, p, state: SolveState, deadline: float | None = None):
+    """``minimization.py:200-253``: AMSgrad steps of orbital rotations (no
+    further steps once ``time.perf_counter()`` passes ``deadline``)."""
     n, _ = nof.ocupacion_softmax(gamma, p)
     cj12, ck12 = nof.cjckd8(n, p)
     np.fill_diagonal(cj12, 0.0)  # as calce / calcorbg do in place
@@ -252,6 +253,8 @@ def orbopt_adam(gamma, C, be, p, state: SolveState):
     best_E, best_C = E, C
     nit = 0
     for i in range(state.maxloop):
+        if deadline is not None and i > 0 and time.perf_counter() > deadline:
+            break
         nit += 1
         grad = nof.orbital_gradient(elag, p)
         if np.linalg.norm(grad) < 1e-4 and improved:
@@ -290,14 +293,24 @@ class SolveResult:
 
 
 def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_switch: float | None = None,
-          callback=None) -> SolveResult:
+          callback=None, ladder=None, final_fp64: bool = False, time_limit: float | None = None) -> SolveResult:
     """The outer loop of ``compute_energy`` (``energy.py:112-170``).
 
     Converged when both gradient norms are below ``tol`` (or their optimizers
-    report success), as ``energy.py:155`` (whose tolerance is 1e-3).  With
-    ``fp64_switch`` set, the backend switches from the mixed path to FP64 once
-    the orbital gradient norm falls below it."""
+    report success), as ``energy.py:155`` (whose tolerance is 1e-3).
+
+    Precision is switched up as the orbital gradient norm falls: ``ladder``
+    is a sequence of (threshold, precision, nslices) rungs taken in order,
+    each once the norm is below its threshold (e.g. bf16x3 digits first, then
+    six digits at 1e-2); ``fp64_switch`` is the one-rung ladder to the FP64
+    path.  With ``final_fp64`` the closing Lagrangian (the reported energy) is
+    evaluated on the FP64 path.  ``time_limit`` (seconds) ends the loop
+    unconverged once it has passed (orbital steps stop at the limit, the outer
+    iteration in progress completes)."""
     t0 = time.perf_counter()
+    rungs = list(ladder or [])
+    if fp64_switch is not None:
+        rungs.append((fp64_switch, "fp64", None))
     p = copy.copy(p)
     state = SolveState(alpha=getattr(p, "alpha", 0.02), maxloop=getattr(p, "maxloop", 30))
     hist = {k: [] for k in ("E_orb", "E_occ", "g_orb", "g_occ", "nit_orb", "nit_occ", "precision")}
@@ -306,8 +319,9 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
     hist["nit_occ"].append(nit_occ)
     converged = False
     it = 0
+    deadline = None if time_limit is None else t0 + time_limit
     for it in range(maxit):
-        E_orb, C, nit_orb, ok_orb = orbopt_adam(gamma, C, be, p, state)
+        E_orb, C, nit_orb, ok_orb = orbopt_adam(gamma, C, be, p, state, deadline=deadline)
         E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
         C, gamma = nof.order_occupations_softmax(C, gamma, p)
         g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
@@ -321,13 +335,18 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
             hist[k].append(v)
         if callback is not None:
             callback(it, hist)
-        if fp64_switch is not None and be.precision != "fp64" and g_orb < fp64_switch:
-            be.set_precision("fp64")
+        while rungs and g_orb < rungs[0][0]:
+            _, prec, ns = rungs.pop(0)
+            be.set_precision(prec, ns)
         if (ok_orb or g_orb < tol) and (ok_occ or g_occ < tol):
             converged = True
             break
+        if time_limit is not None and time.perf_counter() - t0 > time_limit:
+            break
     n, _ = nof.ocupacion_softmax(gamma, p)
     cj12, ck12 = nof.cjckd8(n, p)
+    if final_fp64 and be.precision != "fp64":
+        be.set_precision("fp64")
     elag, Hmat = be.lagrange2(C, n, cj12, ck12)
     P = p.nbf5
     E = float(np.trace(elag[:P, :P]) + np.dot(n[:P], np.diagonal(Hmat)[:P]))
