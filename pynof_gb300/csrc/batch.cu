@@ -10,6 +10,10 @@
 //   1, 2, 3  operands swapped, orbitals on the N side with N tile 32, 64, 128
 //      (small nbf5 then wastes less of each tile).
 // The K phase (a symmetric SYRK per orbital) always uses configuration 0.
+// A phase whose outputs store along the tile rows' unit stride (configuration
+// 3, and K) runs as one persistent launch (one CTA per SM) over the
+// concatenated tile space of all molecules, in order through a tile counter;
+// the others run one CTA per tile.
 #include <cstring>
 #include <new>
 #include <vector>
@@ -126,9 +130,12 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
     pk[i] = OzProblem{w.T, w.T, k};
     tilesK += ozaki_tiles(pk[i].g);
   }
-  GB_TRY(ozaki_group_upload(pt.data(), nmol, tabT));
-  GB_TRY(ozaki_group_upload(pj.data(), nmol, tabJ));
-  GB_TRY(ozaki_group_upload(pk.data(), nmol, tabK));
+  // phases whose outputs store rows along their unit stride (orbitals on the
+  // 128-wide N tile, and K) run as persistent grouped launches
+  bool persT = false, persJ = false, persK = false;
+  GB_TRY(ozaki_group_upload(pt.data(), nmol, tabT, &persT));
+  GB_TRY(ozaki_group_upload(pj.data(), nmol, tabJ, &persJ));
+  GB_TRY(ozaki_group_upload(pk.data(), nmol, tabK, &persK));
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   GB_TRY(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture"));
@@ -136,15 +143,15 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
   auto body = [&]() -> int {
     for (int i = 0; i < nmol; ++i)
       GB_TRY(slice_operand(SliceSrc{C[i], 0, lin(1), lin(nbf[i]), false}, ws[i].A, s));
-    GB_TRY(ozaki_gemm_grouped(tabT, nmol, tilesT, S, pt[0].g.bn, s, "ozaki_tc:batch_half_transform"));
+    GB_TRY(ozaki_gemm_grouped(tabT, nmol, tilesT, S, pt[0].g.bn, s, "ozaki_tc:batch_half_transform", persT));
     for (int i = 0; i < nmol; ++i) {
       GB_TRY(launch_contract_diag(C[i], ws[i].Tf, ws[i].dv, nbf[i], nbf5[i], naux[i], s));
       GB_TRY(slice_operand(SliceSrc{ws[i].dv, 0, lin(naux[i]), lin(1), true}, ws[i].d, s));
     }
-    GB_TRY(ozaki_gemm_grouped(tabJ, nmol, tilesJ, S, pj[0].g.bn, s, "ozaki_tc:batch_J"));
+    GB_TRY(ozaki_gemm_grouped(tabJ, nmol, tilesJ, S, pj[0].g.bn, s, "ozaki_tc:batch_J", persJ));
     for (int i = 0; i < nmol; ++i)
       GB_TRY(slice_operand(SliceSrc{ws[i].Tf, (long long)nbf[i] * naux[i], lin(naux[i]), lin(1), true}, ws[i].T, s));
-    GB_TRY(ozaki_gemm_grouped(tabK, nmol, tilesK, S, 128, s, "ozaki_tc:batch_K"));
+    GB_TRY(ozaki_gemm_grouped(tabK, nmol, tilesK, S, 128, s, "ozaki_tc:batch_K", persK));
     return GB_OK;
   };
   st = body();

@@ -360,6 +360,26 @@ __device__ __forceinline__ void issue_tf32(uint32_t tmem, uint64_t da, uint64_t 
   started = true;
 }
 
+// Problem of global tile u in a grouped launch: the p with starts[p] <= u <
+// starts[p + 1] (always 0 for a single problem, starts == nullptr).
+__device__ __forceinline__ int find_problem(const long long* starts, int nprob, unsigned int u) {
+  if (starts == nullptr || nprob <= 1) return 0;
+  int lo = 0, hi = nprob;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (starts[mid] <= (long long)u) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// The problem a tile belongs to: the table entry of a grouped launch, the
+// launch's own argument otherwise.
+template <bool GROUPED>
+__device__ __forceinline__ const KArgs& prob_ref(const KArgs& a0, const KArgs* probs, int p) {
+  if constexpr (GROUPED) return probs[p];
+  else return a0;
+}
+
 // Local tile index -> (batch, m0, n0).  The dimension with fewer tiles runs
 // fastest, so that the CTAs sharing a block of the large operand run together
 // (that block is read once from HBM, then from L2).  Returns false
@@ -787,10 +807,11 @@ __device__ __forceinline__ void cta_tile(const KArgs& a, int bz, int m0, int n0,
 // releases TMEM as soon as the last chunk is folded into registers, so the
 // next tile's MMAs overlap the conversion and stores.  Pipeline phases
 // (stages, chunks) count on across tiles.
-template <int S, int BN>
-__device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsigned char* smem_raw) {
+template <int S, int BN, bool GROUPED>
+__device__ __forceinline__ void cta_persistent(const KArgs& a0, const KArgs* __restrict__ probs,
+                                               const long long* __restrict__ starts, int nprob, int ntiles,
+                                               unsigned int* counter, unsigned char* smem_raw) {
   using T = TileCfg<BN, 0>;
-  const OzGemm& g = a.g;
   constexpr int gE = (S + 1) < 4 ? (S + 1) : 4;
   constexpr bool has_inexact = (S + 1) > 4;
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -808,10 +829,12 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 2 * STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * STAGES + 5);
   // tile hand-off from the producer to the MMA issuer and the epilogue: a
-  // ring of tile indices (-1 ends the walk) behind full / empty barriers
+  // ring of (problem, tile) indices (tile -1 ends the walk) behind full /
+  // empty barriers
   constexpr int RING = 4;
-  static_assert(2 * STAGES + 6 <= 16 && (24 + RING / 2) * 8 <= 256, "barrier block of smem_bytes");
+  static_assert(2 * STAGES + 6 <= 16 && (24 + RING) * 8 <= 256, "barrier block of smem_bytes");
   volatile int* ring = reinterpret_cast<volatile int*>(bars + 24);
+  volatile int* ringp = ring + RING;
   const uint32_t ringbar0 = smem_u32(bars + 16);
   auto ring_full = [&](int r) { return ringbar0 + 8u * r; };
   auto ring_empty = [&](int r) { return ringbar0 + 8u * (RING + r); };
@@ -851,8 +874,6 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nkb = (g.K + BK - 1) / BK;
-  const int nchunks = (nkb + CH - 1) / CH;
 
   int gkb_issued = 0;  // stages the producer handled, all tiles (its lane 0)
   if (warp == 0) {
@@ -863,16 +884,16 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
       unsigned int next = blockIdx.x;  // static walk when no tile counter is given
       for (int i = 0; !aborted; ++i) {
         const int slot = i % RING;
-        if (!mbar_wait(ring_empty(slot), (uint32_t)(((i / RING) & 1) ^ 1), abort_flag, a.wait_ns)) {
+        if (!mbar_wait(ring_empty(slot), (uint32_t)(((i / RING) & 1) ^ 1), abort_flag, a0.wait_ns)) {
           signal_abort(abort_flag);
           break;
         }
         // next tile that has work (tiles a symmetry skips are passed over here)
-        int t, bz, m0, n0;
+        int t, p = 0, bz, m0, n0;
         for (;;) {
           unsigned int u;
-          if (g.tile_counter) {
-            u = atomicAdd(g.tile_counter, 1u);
+          if (counter) {
+            u = atomicAdd(counter, 1u);
           } else {
             u = next;
             next += gridDim.x;
@@ -881,12 +902,20 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
             t = -1;
             break;
           }
-          t = (int)u;
-          if (decode_tile<BN>(g, t, bz, m0, n0)) break;
+          if constexpr (GROUPED) {
+            p = find_problem(starts, nprob, u);
+            t = (int)(u - starts[p]);
+          } else {
+            t = (int)u;
+          }
+          if (decode_tile<BN>(prob_ref<GROUPED>(a0, probs, p).g, t, bz, m0, n0)) break;
         }
         ring[slot] = t;
+        ringp[slot] = p;
         mbar_arrive(ring_full(slot));
         if (t < 0) break;
+        const KArgs& a = prob_ref<GROUPED>(a0, probs, p);
+        const int nkb = (a.g.K + BK - 1) / BK;
         const long long abz = a.A.batch == 1 ? 0 : bz, bbz = a.B.batch == 1 ? 0 : bz;
         const unsigned char* ga = reinterpret_cast<const unsigned char*>(a.A.planes) + abz * a.A.batch_bytes() +
                                   (long long)(m0 / BM) * a.A.kblocks() * a_bytes;
@@ -896,12 +925,12 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         for (int kb = 0; kb < nkb; ++kb) {
           const int st = gkb % STAGES;
           const uint32_t ph = (uint32_t)((gkb / STAGES) & 1);
-          if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag, a.wait_ns)) {
+          if (!mbar_wait(empty_bar(st), ph ^ 1, abort_flag, a0.wait_ns)) {
             signal_abort(abort_flag);
             aborted = true;
             break;
           }
-          if (gkb == a.withhold && blockIdx.x == 0) {
+          if (gkb == a0.withhold && blockIdx.x == 0) {
             ++gkb;  // test hook: this stage never arrives
             continue;
           }
@@ -930,13 +959,15 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
       bool aborted = false;
       for (int i = 0; !aborted; ++i) {
         const int slot = i % RING;
-        if (!mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a.wait_ns)) {
+        if (!mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a0.wait_ns)) {
           signal_abort(abort_flag);
           break;
         }
-        const int t = ring[slot];
+        const int t = ring[slot], p = ringp[slot];
         mbar_arrive(ring_empty(slot));
         if (t < 0) break;
+        const OzGemm& g = prob_ref<GROUPED>(a0, probs, p).g;
+        const int nkb = (g.K + BK - 1) / BK;
         int bz, m0, n0;
         decode_tile<BN>(g, t, bz, m0, n0);
         const int n_valid = min(BN, g.N - n0);
@@ -944,7 +975,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
         const uint32_t idesc = (T::IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n_mma >> 3) << 17);
         for (int kb = 0; kb < nkb; ++kb) {
           const int st = gkb % STAGES;
-          if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag, a.wait_ns)) {
+          if (!mbar_wait(full_bar(st), (uint32_t)((gkb / STAGES) & 1), abort_flag, a0.wait_ns)) {
             signal_abort(abort_flag);
             aborted = true;
             break;
@@ -959,7 +990,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           // epilogue has taken everything out of TMEM; inside a tile the FP32
           // group may run ahead while the exact groups drain
           if (first && gch > 0 && (c == 0 || g.fdrain)) {
-            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a.wait_ns)) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a0.wait_ns)) {
               signal_abort(abort_flag);
               aborted = true;
               break;
@@ -969,7 +1000,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
           if (first && c > 0 && !g.fdrain) {
             // the FP32 group runs ahead while the exact groups drain
             issue_products<S, BN, 1>(tmem, da, db, idesc, false, false);
-            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a.wait_ns)) {
+            if (!mbar_wait(accempty_bar, (uint32_t)((gch - 1) & 1), abort_flag, a0.wait_ns)) {
               signal_abort(abort_flag);
               aborted = true;
               break;
@@ -998,21 +1029,25 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
     const int cg = (warp - 2) >> 2;
     const int et = threadIdx.x - 64;
     const uint32_t lbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cg * CW);
-    const float two_frac = __int_as_float((127 + a.frac) << 23);
     const float upE = __int_as_float((127 + 7 * gE) << 23);
     const int row = q * 32 + lane;
     int gch = 0;
     for (int i = 0;; ++i) {
       const int slot = i % RING;
-      const bool got = mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a.wait_ns);
+      const bool got = mbar_wait(ring_full(slot), (uint32_t)((i / RING) & 1), abort_flag, a0.wait_ns);
       if (!got) signal_abort(abort_flag);
       const int t = got ? ring[slot] : -1;
+      const int p = got ? ringp[slot] : 0;
       __syncwarp();
       if (lane == 0) mbar_arrive(ring_empty(slot));
       // every epilogue warp is done with the previous tile's tables, and all
       // of them take the same branch
       if (epi_barrier_any(!got || *abort_flag != 0)) break;
       if (t < 0) break;
+      const KArgs& a = prob_ref<GROUPED>(a0, probs, p);
+      const OzGemm& g = a.g;
+      const int nchunks = ((g.K + BK - 1) / BK + CH - 1) / CH;
+      const float two_frac = __int_as_float((127 + a.frac) << 23);  // 2^frac
       int bz, m0, n0;
       decode_tile<BN>(g, t, bz, m0, n0);
       {
@@ -1057,7 +1092,7 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
       for (int j = 0; j < CW; ++j) R[j] = 0;
       bool ok = true;
       for (int c = 0; c < nchunks; ++c) {
-        const bool got = mbar_wait(accfull_bar, (uint32_t)(gch & 1), abort_flag, a.wait_ns);
+        const bool got = mbar_wait(accfull_bar, (uint32_t)(gch & 1), abort_flag, a0.wait_ns);
         if (!__all_sync(0xffffffffu, got)) {
           signal_abort(abort_flag);
           ok = false;
@@ -1121,10 +1156,10 @@ __device__ __forceinline__ void cta_persistent(const KArgs& a, int ntiles, unsig
   // after an abort, the producer's copies land before the CTA exits
   if (warp == 0 && lane == 0 && *abort_flag) {
     for (int k = gkb_issued > STAGES ? gkb_issued - STAGES : 0; k < gkb_issued; ++k)
-      mbar_wait(full_bar(k % STAGES), (uint32_t)((k / STAGES) & 1), nullptr, a.wait_ns);
+      mbar_wait(full_bar(k % STAGES), (uint32_t)((k / STAGES) & 1), nullptr, a0.wait_ns);
   }
   if (warp == 1) {
-    if (*abort_flag) mbar_wait(done_bar, 0, nullptr, a.wait_ns);
+    if (*abort_flag) mbar_wait(done_bar, 0, nullptr, a0.wait_ns);
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(T::TMEM_COLS) : "memory");
   }
@@ -1134,7 +1169,19 @@ template <int S, int BN>
 __global__ void __maxnreg__(MAX_REGS) ozaki_persistent_kernel(const __grid_constant__ KArgs a, int ntiles) {
   extern __shared__ unsigned char smem_raw[];
   if (*(volatile int*)&g_tc_status != 0) return;
-  cta_persistent<S, BN>(a, ntiles, smem_raw);
+  cta_persistent<S, BN, false>(a, nullptr, nullptr, 1, ntiles, a.g.tile_counter, smem_raw);
+}
+
+// Grouped persistent launch: problem p owns the tiles [starts[p], starts[p + 1])
+// of one tile space walked in order through `counter` (caller memory, zeroed
+// before the launch), one CTA per SM.
+template <int S, int BN>
+__global__ void __maxnreg__(MAX_REGS)
+    ozaki_persistent_grouped_kernel(const KArgs* __restrict__ probs, const long long* __restrict__ starts, int nprob,
+                                    int ntiles, unsigned int* counter) {
+  extern __shared__ unsigned char smem_raw[];
+  if (*(volatile int*)&g_tc_status != 0) return;
+  cta_persistent<S, BN, true>(probs[0], probs, starts, nprob, ntiles, counter, smem_raw);
 }
 
 template <int S, int BN, int KIND>
@@ -1218,6 +1265,18 @@ PersistFn persistent_for(int S) {
   }
 }
 
+using PersistGroupedFn = void (*)(const KArgs*, const long long*, int, int, unsigned int*);
+PersistGroupedFn persistent_grouped_for(int S) {
+  switch (S) {
+    case 1: return ozaki_persistent_grouped_kernel<1, 128>;
+    case 2: return ozaki_persistent_grouped_kernel<2, 128>;
+    case 3: return ozaki_persistent_grouped_kernel<3, 128>;
+    case 4: return ozaki_persistent_grouped_kernel<4, 128>;
+    case 5: return ozaki_persistent_grouped_kernel<5, 128>;
+    default: return ozaki_persistent_grouped_kernel<6, 128>;
+  }
+}
+
 KernelFn kernel_for(int S, int BN) {
   return BN == 32 ? single_for<32>(S) : BN == 64 ? single_for<64>(S) : single_for<128>(S);
 }
@@ -1246,10 +1305,14 @@ int configure_device() {
           cudaFuncSetAttribute(grouped_kernel_for(sl, bn), cudaFuncAttributeMaxDynamicSharedMemorySize, sm),
           "cudaFuncSetAttribute"));
     }
-  for (int sl = 1; sl <= 6; ++sl)
+  for (int sl = 1; sl <= 6; ++sl) {
     GB_TRY(cuda_status(cudaFuncSetAttribute(persistent_for(sl), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem_bytes(sl, 128)),
                        "cudaFuncSetAttribute"));
+    GB_TRY(cuda_status(cudaFuncSetAttribute(persistent_grouped_for(sl), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem_bytes(sl, 128)),
+                       "cudaFuncSetAttribute"));
+  }
   GB_TRY(cuda_status(cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev),
                      "cudaDeviceGetAttribute"));
   configured[dev] = current_context_id();
@@ -1356,21 +1419,30 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
   return GB_OK;
 }
 
+// table layout: KArgs[nprob] | starts[nprob + 1] | tile counter
 size_t ozaki_group_table_bytes(int nprob) {
-  return align256((size_t)nprob * sizeof(KArgs)) + align256((size_t)(nprob + 1) * sizeof(long long));
+  return align256((size_t)nprob * sizeof(KArgs)) + align256((size_t)(nprob + 1) * sizeof(long long)) + 256;
 }
 
-int ozaki_group_upload(const OzProblem* probs, int nprob, void* table) {
+int ozaki_group_upload(const OzProblem* probs, int nprob, void* table, bool* persistent) {
   GB_REQUIRE(nprob >= 1 && probs && table, GB_ERR_INVALID_ARG, "ozaki_group_upload: empty group");
   std::vector<KArgs> args;
   std::vector<long long> starts(1, 0);
+  bool all_rows_fast = true;
   for (int i = 0; i < nprob; ++i) {
     GB_TRY(check_problem(probs[i].A, probs[i].B, probs[i].g));
     GB_REQUIRE(probs[i].g.S == probs[0].g.S && probs[i].g.bn == probs[0].g.bn, GB_ERR_INVALID_ARG,
                "ozaki_group_upload: a group shares one slice count and tile width");
     args.push_back(make_args(probs[i].A, probs[i].B, probs[i].g));
     starts.push_back(starts.back() + ozaki_tiles(probs[i].g));
+    const OzGemm& g = probs[i].g;
+    all_rows_fast = all_rows_fast && !(g.c_c.div == 0 && g.c_c.s0 == 1) && (g.c_r.div == 0 && g.c_r.s0 == 1);
   }
+  // the persistent form stores from the epilogue's registers: every output's
+  // tile rows must be its unit stride; bf16 digits and 128-wide tiles
+  if (persistent)
+    *persistent = all_rows_fast && probs[0].g.S >= 1 && probs[0].g.S <= 6 && probs[0].g.bn == 128 &&
+                  starts.back() < (1LL << 30);
   char* t = static_cast<char*>(table);
   GB_TRY(cuda_status(cudaMemcpy(t, args.data(), nprob * sizeof(KArgs), cudaMemcpyHostToDevice), "group table"));
   GB_TRY(cuda_status(cudaMemcpy(t + align256((size_t)nprob * sizeof(KArgs)), starts.data(),
@@ -1380,12 +1452,30 @@ int ozaki_group_upload(const OzProblem* probs, int nprob, void* table) {
 }
 
 int ozaki_gemm_grouped(const void* table, int nprob, long long total_tiles, int S, int bn, cudaStream_t stream,
-                       const char* tag) {
+                       const char* tag, bool persistent) {
   if (total_tiles <= 0) return GB_OK;
   GB_TRY(configure_device());
   const char* t = static_cast<const char*>(table);
   const KArgs* probs = reinterpret_cast<const KArgs*>(t);
-  const long long* starts = reinterpret_cast<const long long*>(t + align256((size_t)nprob * sizeof(KArgs)));
+  const size_t off_starts = align256((size_t)nprob * sizeof(KArgs));
+  const long long* starts = reinterpret_cast<const long long*>(t + off_starts);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int nsm = (dev >= 0 && dev < 64 && g_num_sms[dev] > 0) ? g_num_sms[dev] : 0;
+  if (persistent && S >= 1 && S <= 6 && bn == 128 && nsm > 0 && total_tiles < (1LL << 30)) {
+    // one CTA per SM walking the concatenated tile space in order
+    unsigned int* counter = reinterpret_cast<unsigned int*>(
+        const_cast<char*>(t) + off_starts + align256((size_t)(nprob + 1) * sizeof(long long)));
+    const long long grid = total_tiles < nsm ? total_tiles : nsm;
+    GB_TRY(cuda_status(cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream), "grouped tile counter"));
+    const int pi = prof_begin(tag, stream);
+    persistent_grouped_for(S)<<<(unsigned)grid, THREADS, smem_bytes(S, 128), stream>>>(probs, starts, nprob,
+                                                                                      (int)total_tiles, counter);
+    prof_end(pi, stream);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) return launch_error(tag, le, S, 128);
+    return GB_OK;
+  }
   const int pi = prof_begin(tag, stream);
   grouped_kernel_for(S, bn)<<<grid_for(total_tiles), THREADS, smem_bytes(S, bn), stream>>>(probs, starts, nprob);
   prof_end(pi, stream);

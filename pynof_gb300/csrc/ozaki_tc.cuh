@@ -56,10 +56,14 @@ int ozaki_gemm(const SlicedDesc& A, const SlicedDesc& B, const OzGemm& g, cudaSt
 // is caller device memory of ozaki_group_table_bytes(n) bytes; it is filled
 // here with a synchronous copy, so a grouped launch can be captured into a
 // CUDA graph once the table holds the problem list.
+// With `persistent` set by the upload (every output's tile rows are its unit
+// stride, bf16 digits, 128-wide tiles) and passed to the launch, the group
+// runs as one persistent launch (one CTA per SM) walking the concatenated
+// tile space in order through a counter in the table; otherwise one CTA per tile.
 size_t ozaki_group_table_bytes(int nprob);
-int ozaki_group_upload(const OzProblem* probs, int nprob, void* table);
+int ozaki_group_upload(const OzProblem* probs, int nprob, void* table, bool* persistent = nullptr);
 int ozaki_gemm_grouped(const void* table, int nprob, long long total_tiles, int S, int bn, cudaStream_t stream,
-                       const char* tag);
+                       const char* tag, bool persistent = false);
 // Tiles of one problem (for building the grouped tile ranges).
 long long ozaki_tiles(const OzGemm& g);
 
