@@ -62,6 +62,7 @@ def parse():
                          "precision: every split form against FP64 (J, K, E, orbital gradient); "
                          "mo: computeJKH_MO and computeLagrange2 per kernel, with the bandwidth kernels' GB/s")
     ap.add_argument("--nmol", type=int, default=64)
+    ap.add_argument("--batch-nbf-max", type=int, default=400, help="largest nbf of the batch (batch mode)")
     ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rate", type=float, default=10.0)
     ap.add_argument("--nbf-min", type=int, default=24)
@@ -492,7 +493,7 @@ def run_batch(args):
     from pynof_gb300 import ops, synthetic
 
     torch.cuda.set_device(0)
-    sizes = synthetic.batch_sizes(args.nmol)
+    sizes = synthetic.batch_sizes(args.nmol, hi=args.batch_nbf_max)
     mols, fp64_in = [], []
     for i, nbf in enumerate(sizes):
         st = synthetic.Structure.for_nbf(nbf)
@@ -535,7 +536,8 @@ def run_batch(args):
         J64, K64 = ops.jkj_ri(c, bb, p)
         err = max(err, float((J - J64).abs().max() / J64.abs().max()), float((K - K64).abs().max() / K64.abs().max()))
     nm = len(mols)
-    line = {"metric": "batched RI-JK builds/s, 64 molecules nbf log-uniform in [24,400]", "unit": "builds/s",
+    line = {"metric": f"batched RI-JK builds/s, {args.nmol} molecules nbf log-uniform in [24,{args.batch_nbf_max}]",
+            "unit": "builds/s",
             "value": nm / tgr, "steps": args.steps, "dtype": "bf16-split-f64", "data": "synthetic",
             "config": {"workload": f"{nm} molecules, nbf {min(sizes)}..{max(sizes)} (median "
                                    f"{int(np.median(sizes))}), naux=4 nbf, nbf5=5 (nbf//10)",

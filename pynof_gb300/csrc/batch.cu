@@ -2,7 +2,8 @@
 // the three GEMM phases of every molecule (half transform, J, K) each run as
 // ONE grouped launch over all molecules' tiles, and the whole sequence --
 // per-molecule slicing and diagonal kernels included -- is captured once into
-// a CUDA graph that gb_batch_launch replays.
+// a CUDA graph that gb_batch_launch replays (the per-molecule kernels as
+// parallel branches of the graph).
 //
 // Tile configuration per phase (chosen by the caller, e.g. the autotuner in
 // pynof_gb300/batch.py):
@@ -138,25 +139,70 @@ extern "C" int gb_jkj_batch_create_mixed(int nmol, const double* const* C, const
   GB_TRY(ozaki_group_upload(pk.data(), nmol, tabK, &persK));
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The per-molecule kernels between the grouped GEMMs (slicing, the diagonal
+  // contraction) are small; they are captured as parallel branches on
+  // kBranches forked streams (molecule i on branch i % kBranches), so the
+  // replay runs several molecules' kernels at once instead of one after another.
+  constexpr int kBranches = 8;
+  const int nbr = nmol < kBranches ? nmol : kBranches;
+  cudaStream_t aux[kBranches] = {};
+  cudaEvent_t ev[4 * (kBranches + 1)] = {};
+  auto release = [&]() {
+    for (cudaEvent_t& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (cudaStream_t& a : aux)
+      if (a) cudaStreamDestroy(a);
+  };
+  for (int j = 0; j < nbr; ++j) {
+    const cudaError_t e = cudaStreamCreateWithFlags(&aux[j], cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      release();
+      return cuda_status(e, "gb_jkj_batch_create_mixed: branch streams");
+    }
+  }
+  for (cudaEvent_t& e : ev) {
+    const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (r != cudaSuccess) {
+      release();
+      return cuda_status(r, "gb_jkj_batch_create_mixed: branch events");
+    }
+  }
+  int phase = 0;
+  // run per_mol(i, stream) for every molecule on the branches, between a fork
+  // from and a join back into the capturing stream
+  auto branches = [&](auto&& per_mol) -> int {
+    cudaEvent_t* pe = ev + (phase++) * (kBranches + 1);
+    GB_TRY(cuda_status(cudaEventRecord(pe[0], s), "batch fork"));
+    for (int j = 0; j < nbr; ++j) GB_TRY(cuda_status(cudaStreamWaitEvent(aux[j], pe[0], 0), "batch fork"));
+    for (int i = 0; i < nmol; ++i) GB_TRY(per_mol(i, aux[i % nbr]));
+    for (int j = 0; j < nbr; ++j) {
+      GB_TRY(cuda_status(cudaEventRecord(pe[1 + j], aux[j]), "batch join"));
+      GB_TRY(cuda_status(cudaStreamWaitEvent(s, pe[1 + j], 0), "batch join"));
+    }
+    return GB_OK;
+  };
   GB_TRY(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture"));
   int st = GB_OK;
   auto body = [&]() -> int {
-    for (int i = 0; i < nmol; ++i)
-      GB_TRY(slice_operand(SliceSrc{C[i], 0, lin(1), lin(nbf[i]), false}, ws[i].A, s));
+    GB_TRY(branches([&](int i, cudaStream_t b) {
+      return slice_operand(SliceSrc{C[i], 0, lin(1), lin(nbf[i]), false}, ws[i].A, b);
+    }));
     GB_TRY(ozaki_gemm_grouped(tabT, nmol, tilesT, S, pt[0].g.bn, s, "ozaki_tc:batch_half_transform", persT));
-    for (int i = 0; i < nmol; ++i) {
-      GB_TRY(launch_contract_diag(C[i], ws[i].Tf, ws[i].dv, nbf[i], nbf5[i], naux[i], s));
-      GB_TRY(slice_operand(SliceSrc{ws[i].dv, 0, lin(naux[i]), lin(1), true}, ws[i].d, s));
-    }
+    GB_TRY(branches([&](int i, cudaStream_t b) {
+      GB_TRY(launch_contract_diag(C[i], ws[i].Tf, ws[i].dv, nbf[i], nbf5[i], naux[i], b));
+      return slice_operand(SliceSrc{ws[i].dv, 0, lin(naux[i]), lin(1), true}, ws[i].d, b);
+    }));
     GB_TRY(ozaki_gemm_grouped(tabJ, nmol, tilesJ, S, pj[0].g.bn, s, "ozaki_tc:batch_J", persJ));
-    for (int i = 0; i < nmol; ++i)
-      GB_TRY(slice_operand(SliceSrc{ws[i].Tf, (long long)nbf[i] * naux[i], lin(naux[i]), lin(1), true}, ws[i].T, s));
+    GB_TRY(branches([&](int i, cudaStream_t b) {
+      return slice_operand(SliceSrc{ws[i].Tf, (long long)nbf[i] * naux[i], lin(naux[i]), lin(1), true}, ws[i].T, b);
+    }));
     GB_TRY(ozaki_gemm_grouped(tabK, nmol, tilesK, S, 128, s, "ozaki_tc:batch_K", persK));
     return GB_OK;
   };
   st = body();
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+  release();
   if (st != GB_OK) {
     if (graph) cudaGraphDestroy(graph);
     return st;
