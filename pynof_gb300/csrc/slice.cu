@@ -14,12 +14,15 @@ __device__ __forceinline__ int exponent_of(unsigned long long maxbits) {
   return (ex == 0 ? 1 : ex) - 1022;
 }
 
-// Balanced base-128 digits of round(x 2^(7S - E)), stored pre-weighted as bf16
-// bit patterns.  Every digit value d 2^(-7 s) (|d| <= 128) is exact in bf16, so
-// its bf16 bits are the upper half of its FP32 bits; FP32 values come from
-// the integer with the 1.5 * 2^23 magic-number trick (exact for |d| < 2^22).
+// Balanced base-128 digits of round(x 2^(7S - E)), pre-weighted: digit s as
+// the FP32 bits of d 2^(-7 s) (|d| <= 128, exact in bf16, so the upper half of
+// those bits is the bf16 pattern; the lower half is zero).  The 64-bit integer
+// xi = H 2^(7 NL) + L (0 <= L < 2^(7 NL)) is taken apart in 32-bit pieces: the
+// NL lowest digits come from L (its carry, 0 or 1, goes to H), the others from
+// H.  Each digit's FP32 value comes from the 1.5 * 2^23 magic number (exact for
+// |d| < 2^22), scaled by 2^(-7 s) in the same (exact) fused multiply-add.
 template <int S>
-__device__ __forceinline__ void make_digits(double x, int E, unsigned short* out) {
+__device__ __forceinline__ void make_digits(double x, int E, uint32_t* out) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   int ex = (int)((bits >> 52) & 0x7FF);
   unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
@@ -30,15 +33,26 @@ __device__ __forceinline__ void make_digits(double x, int E, unsigned short* out
   else if (r >= 64) xi = 0;
   else xi = (long long)((m + (1ull << (r - 1))) >> r);
   if (bits >> 63) xi = -xi;
+  constexpr int NL = S - 1 < 3 ? S - 1 : 3;
+  int L = (int)(xi & ((1ll << (7 * NL)) - 1));
+  int H = (int)(xi >> (7 * NL));
 #pragma unroll
-  for (int s = S; s >= 2; --s) {
-    const int d = (((int)xi + 64) & 127) - 64;
-    xi = (xi - d) >> 7;
-    const float f = (__int_as_float(0x4B400000 + d) - 12582912.0f) * __int_as_float((127 - 7 * s) << 23);
-    out[s - 1] = (unsigned short)(__float_as_uint(f) >> 16);
+  for (int s = S; s > S - NL; --s) {
+    const int d = ((L + 64) & 127) - 64;
+    L = (L - d) >> 7;
+    const float w = __int_as_float((127 - 7 * s) << 23);
+    out[s - 1] = __float_as_uint(fmaf(__int_as_float(0x4B400000 + d), w, -12582912.0f * w));
   }
-  const float f1 = (__int_as_float(0x4B400000 + (int)xi) - 12582912.0f) * __int_as_float((127 - 7) << 23);
-  out[0] = (unsigned short)(__float_as_uint(f1) >> 16);
+  H += L;
+#pragma unroll
+  for (int s = S - NL; s >= 2; --s) {
+    const int d = ((H + 64) & 127) - 64;
+    H = (H - d) >> 7;
+    const float w = __int_as_float((127 - 7 * s) << 23);
+    out[s - 1] = __float_as_uint(fmaf(__int_as_float(0x4B400000 + d), w, -12582912.0f * w));
+  }
+  const float w1 = __int_as_float((127 - 7) << 23);
+  out[0] = __float_as_uint(fmaf(__int_as_float(0x4B400000 + H), w1, -12582912.0f * w1));
 }
 
 // A NaN or an infinity has the largest magnitude bits of all; it has no digits,
@@ -71,19 +85,31 @@ __global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restri
   }
 }
 
-// One thread per row; rows are the unit-stride index.
-__global__ void rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps, int* status) {
+// Rows are the unit-stride index: 32 consecutive rows per CTA (lane = row,
+// each warp reads 256 contiguous bytes per k) and its 8 warps split K; the
+// partial maxima meet in shared memory.
+__global__ void __launch_bounds__(256) rowexp_rfast_kernel(SliceSrc src, int rows, int K, int* __restrict__ exps,
+                                                           int* status) {
+  __shared__ unsigned long long part[8][32];
   const long long b = blockIdx.y;
-  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= rows) return;
-  const double* base = src.p + b * src.sb + src.row_at(row);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long row = (long long)blockIdx.x * 32 + lane;
   unsigned long long mx = 0;
-  for (int k = 0; k < K; ++k) {
-    const unsigned long long v = abs_bits(base[src.k.at(k)]);
-    mx = v > mx ? v : mx;
+  if (row < rows) {
+    const double* base = src.p + b * src.sb + src.row_at(row);
+    for (int k = w; k < K; k += 8) {
+      const unsigned long long v = abs_bits(base[src.k.at(k)]);
+      mx = v > mx ? v : mx;
+    }
   }
-  exps[b * rows + row] = exponent_of(mx);
-  note_nonfinite(mx, status);
+  part[w][lane] = mx;
+  __syncthreads();
+  if (w == 0 && row < rows) {
+#pragma unroll
+    for (int j = 1; j < 8; ++j) mx = part[j][lane] > mx ? part[j][lane] : mx;
+    exps[b * rows + row] = exponent_of(mx);
+    note_nonfinite(mx, status);
+  }
 }
 
 // k blocks per CTA of the digit slicer
@@ -117,11 +143,12 @@ __device__ __forceinline__ void store_group(const double (&xs)[8], int e, unsign
   uint32_t pk[S][4];
 #pragma unroll
   for (int u = 0; u < 8; u += 2) {
-    unsigned short d0[S], d1[S];
+    uint32_t d0[S], d1[S];
     make_digits<S>(xs[u], e, d0);
     make_digits<S>(xs[u + 1], e, d1);
+    // the two bf16 patterns (upper halves) side by side
 #pragma unroll
-    for (int s = 0; s < S; ++s) pk[s][u >> 1] = (uint32_t)d0[s] | ((uint32_t)d1[s] << 16);
+    for (int s = 0; s < S; ++s) pk[s][u >> 1] = __byte_perm(d0[s], d1[s], 0x7632);
   }
 #pragma unroll
   for (int s = 0; s < S; ++s)
@@ -250,8 +277,8 @@ int slice_operand(const SliceSrc& src, const SlicedDesc& dst, cudaStream_t s, bo
   } else {
     int* st = device_status_word();
     GB_LAUNCH("slice_rowexp", s,
-              rowexp_rfast_kernel<<<dim3(cdiv(dst.rows, 256), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K,
-                                                                                      dst.exps, st));
+              rowexp_rfast_kernel<<<dim3(cdiv(dst.rows, 32), dst.batch), 256, 0, s>>>(src, dst.rows, dst.K,
+                                                                                     dst.exps, st));
   }
   const long long blocks = (long long)dst.rblocks() * dst.kblocks();
   GB_REQUIRE(blocks <= 2147483647LL, GB_ERR_BAD_SHAPE, "slice_operand: too many blocks");
