@@ -57,10 +57,11 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
-    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision", "mo"], default="jk",
+    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision", "mo", "hostlink"], default="jk",
                     help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream; "
                          "precision: every split form against FP64 (J, K, E, orbital gradient); "
-                         "mo: computeJKH_MO and computeLagrange2 per kernel, with the bandwidth kernels' GB/s")
+                         "mo: computeJKH_MO and computeLagrange2 per kernel, with the bandwidth kernels' GB/s; "
+                         "hostlink: device <-> pinned host copy rates at the size of one build's J, K")
     ap.add_argument("--nmol", type=int, default=64)
     ap.add_argument("--batch-nbf-max", type=int, default=400, help="largest nbf of the batch (batch mode)")
     ap.add_argument("--requests", type=int, default=16)
@@ -309,8 +310,11 @@ def run_ours(args):
     del Jh, Kh
     barrier()
     t0 = time.perf_counter()
+    step_s = []
     for _ in range(args.steps):
+        ts = time.perf_counter()
         Jh, Kh = integrals.JKj_RI_GPU(C_pin, db, p)
+        step_s.append(time.perf_counter() - ts)
     barrier()
     e2e_value, e2e_s = reps.throughput(args.steps, time.perf_counter() - t0)
     h2d = C.nbytes
@@ -452,7 +456,9 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (b = %.1f GB)" % (b.nbytes / 1e9),
                    "parallelism": f"replicas x{world}",
                    "prepare_s": round(prep_s, 4)},
-        "e2e": {"value": e2e_value, "unit": "builds/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": "builds/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": {"median": 1e3 * statistics.median(step_s), "min": 1e3 * min(step_s),
+                                "max": 1e3 * max(step_s)}},
         "roofline": roof,
         "gpu_launches": sum(v[0] for v in prof.values()),
         "clocks": clk,
@@ -773,6 +779,47 @@ def run_mo(args):
     print(json.dumps(line), flush=True)
 
 
+def run_hostlink(args):
+    """Copy rates between HBM and pinned host memory at the size of one
+    nbf=600 build's J and K (2 x 864 MB), the transfer the e2e leg makes: one
+    copy stream, two copy streams (one per array), and a device -> host copy
+    after a device kernel has written the buffer (as in the build).  CUDA
+    events on the copy streams, best of --steps.  Also the host's NUMA nodes
+    and this process's CPU set."""
+    import torch
+
+    torch.cuda.set_device(0)
+    n = 300 * 600 * 600
+    dev = [torch.empty(n, dtype=torch.float64, device="cuda").fill_(1.0) for _ in range(2)]
+    host = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+    streams = [torch.cuda.Stream() for _ in range(2)]
+    nbytes = 2 * n * 8
+
+    def timed(two_streams: bool, d2h: bool):
+        best = float("inf")
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for i in range(2):
+                st = streams[i if two_streams else 0]
+                with torch.cuda.stream(st):
+                    (host[i].copy_(dev[i], non_blocking=True) if d2h else dev[i].copy_(host[i], non_blocking=True))
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return nbytes / best / 1e9
+
+    for _ in range(2):
+        timed(False, True)
+    out = {"d2h_gbs_one_stream": timed(False, True), "d2h_gbs_two_streams": timed(True, True),
+           "h2d_gbs_one_stream": timed(False, False), "h2d_gbs_two_streams": timed(True, False)}
+    nodes = sorted(d for d in os.listdir("/sys/devices/system/node") if d.startswith("node")) \
+        if os.path.isdir("/sys/devices/system/node") else []
+    line = {"mode": "hostlink", "bytes_per_copy": nbytes, "unit": "GB/s", "steps": args.steps,
+            "numa_nodes": nodes, "cpus_of_process": len(os.sched_getaffinity(0)),
+            "pinned": "torch pin_memory (cudaHostAlloc)", **out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -785,6 +832,8 @@ def main():
         run_precision(args)
     elif args.mode == "mo":
         run_mo(args)
+    elif args.mode == "hostlink":
+        run_hostlink(args)
     else:
         run_ours(args)
 

@@ -344,6 +344,19 @@ int gb_jkj_ri_mixed_j(const double* C, const void* prep, int nbf, int nbf5, int 
 int gb_jkj_ri_mixed_k(int nbf, int nbf5, int naux, int nslices, int q0, int q1, double* K, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* The same build in finer parts, so that the copies of J and K to the host
+ * can start soon after T is formed and run back to back (the drop-in
+ * JKj_RI_GPU interleaves J and K ranges on one stream and copies each on a
+ * second).  No counterpart in the reference.  gb_jkj_ri_mixed_t forms T and
+ * d and leaves them (and T's slicing exponents) in the workspace;
+ * gb_jkj_ri_mixed_jr then forms J[q] for q0 <= q < q1, q0 a multiple of 128,
+ * and gb_jkj_ri_mixed_k K[q] for any range, in any order, on the same stream
+ * and workspace.  Results are bitwise those of gb_jkj_ri_mixed. */
+int gb_jkj_ri_mixed_t(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices, void* workspace,
+                      size_t workspace_bytes, void* stream);
+int gb_jkj_ri_mixed_jr(const void* prep, int nbf, int nbf5, int naux, int nslices, int q0, int q1, double* J,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
 /* A3  computeJKH_MO, RI, on the tensor cores (same outputs as gb_jkh_mo_ri_f64).
  *     Replaces JKH_MO_RI_GPU (pynof/integrals.py:383-399). */
 size_t gb_jkh_mo_ri_workspace_mixed(int nbf, int nbf5, int naux, int nslices);

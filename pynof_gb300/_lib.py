@@ -87,6 +87,8 @@ SIGNATURES = {
     "gb_jkj_ri_mixed": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
     "gb_jkj_ri_mixed_j": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_jkj_ri_mixed_k": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
+    "gb_jkj_ri_mixed_t": (_I, [_P, _P, _I, _I, _I, _I, _P, _Z, _P]),
+    "gb_jkj_ri_mixed_jr": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _P, _Z, _P]),
     "gb_jkj_batch_workspace_mixed": (_Z, [_I, _P, _P, _P, _I]),
     "gb_jkj_batch_create_mixed": (_I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _Z, _P, _P]),
     "gb_batch_launch": (_I, [_P, _P]),

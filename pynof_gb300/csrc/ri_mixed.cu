@@ -124,30 +124,47 @@ extern "C" size_t gb_jkj_ri_workspace_mixed(int nbf, int nbf5, int naux, int nsl
 }
 
 namespace {
-// The J half of the build: slices C^T, forms T (half transform), d and J.
-// Leaves T and the row exponents of its slicing in the workspace for
-// jkj_mixed_k.
-int jkj_mixed_j(const double* C, const Prepared& pr, const JkjMixedWs& w, int N, int P, int Q, int S, double* J,
-                cudaStream_t s) {
+// The build's prelude: slices C^T, forms T (half transform) and d, slices d.
+// Leaves T, d's slices and the row exponents of T's slicing in the
+// workspace for jkj_mixed_jr and jkj_mixed_k.
+int jkj_mixed_t(const double* C, const Prepared& pr, const JkjMixedWs& w, int N, int P, int Q, cudaStream_t s) {
   // A rows q over K = m: element C[m][q]
   GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.A, s));
   // T[q][(n,l)] = sum_m C[m][q] b[m][(n,l)]
   GB_TRY(half_transform_gemm(w.A, pr.bT, N, P, Q, w.Tf, w.ctr, s));
   // the contraction also records the row exponents of T's slicing (jkj_mixed_k)
   GB_TRY(launch_contract_diag(C, w.Tf, w.dv, N, P, Q, s, w.T.kind == 0 ? w.T.exps : nullptr));
-  // J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l]
-  GB_TRY(slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s));
-  // (bJ's rows are the pairs m <= n; each result is also written to (n, m))
+  return slice_operand(SliceSrc{w.dv, 0, lin(Q), lin(1), true}, w.d, s);
+}
+
+// J[q][(m,n)] = sum_l d[q][l] b[(m,n)][l] for orbitals q0 <= q < q1 (q0 a
+// multiple of the 128-row slice block, so the range starts a block of d's
+// slices).  bJ's rows are the pairs m <= n; each result is also written to (n, m).
+int jkj_mixed_jr(const Prepared& pr, const JkjMixedWs& w, int N, int P, int Q, int S, int q0, int q1, double* J,
+                 cudaStream_t s) {
+  if (q1 <= q0) return GB_OK;
+  SlicedDesc d = w.d;
+  d.planes = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<unsigned char*>(w.d.planes) +
+                                              (size_t)(q0 / SL_ROWS) * (size_t)w.d.kblocks() * w.d.block_bytes());
+  d.exps = w.d.exps + q0;
+  d.rows = q1 - q0;
   OzGemm gj{};
-  gj.K = Q; gj.batch = 1; gj.S = S; gj.C = J; gj.c_sb = 0; gj.pair_n = N; gj.tag = "ozaki_tc:J";
+  gj.K = Q; gj.batch = 1; gj.S = S; gj.C = J + (size_t)q0 * N * N; gj.c_sb = 0; gj.pair_n = N; gj.tag = "ozaki_tc:J";
   gj.tile_counter = w.ctr;
   const int npairs = N * (N + 1) / 2;
   if (orbitals_on_n(P, npairs)) {
-    gj.M = npairs; gj.N = P; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_TRIROW;
-    return ozaki_gemm(pr.bJ, w.d, gj, s);
+    gj.M = npairs; gj.N = q1 - q0; gj.c_r = lin(1); gj.c_c = lin((long long)N * N); gj.sym = SYM_TRIROW;
+    return ozaki_gemm(pr.bJ, d, gj, s);
   }
-  gj.M = P; gj.N = npairs; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_TRICOL;
-  return ozaki_gemm(w.d, pr.bJ, gj, s);
+  gj.M = q1 - q0; gj.N = npairs; gj.c_r = lin((long long)N * N); gj.c_c = lin(1); gj.sym = SYM_TRICOL;
+  return ozaki_gemm(d, pr.bJ, gj, s);
+}
+
+// The J half of the build: the prelude, then J for every orbital.
+int jkj_mixed_j(const double* C, const Prepared& pr, const JkjMixedWs& w, int N, int P, int Q, int S, double* J,
+                cudaStream_t s) {
+  GB_TRY(jkj_mixed_t(C, pr, w, N, P, Q, s));
+  return jkj_mixed_jr(pr, w, N, P, Q, S, 0, P, J, s);
 }
 
 // The K half for orbitals q0 <= q < q1: K[q] = T_q T_q^T from the T that
@@ -208,6 +225,39 @@ extern "C" int gb_jkj_ri_mixed_j(const double* C, const void* prep, int nbf, int
   JkjMixedWs w;
   jkj_mixed_layout(wc, N, P, Q, S, &w);
   return jkj_mixed_j(C, pr, w, N, P, Q, S, J, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gb_jkj_ri_mixed_t(const double* C, const void* prep, int nbf, int nbf5, int naux, int nslices,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(jkj_mixed_check("gb_jkj_ri_mixed_t", N, P, Q, S, workspace_bytes));
+  GB_REQUIRE(C && prep && workspace, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed_t: null pointer");
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  return jkj_mixed_t(C, pr, w, N, P, Q, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gb_jkj_ri_mixed_jr(const void* prep, int nbf, int nbf5, int naux, int nslices, int q0, int q1,
+                                  double* J, void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  const int N = nbf, P = nbf5, Q = naux, S = nslices;
+  GB_TRY(jkj_mixed_check("gb_jkj_ri_mixed_jr", N, P, Q, S, workspace_bytes));
+  GB_REQUIRE(prep && J && workspace, GB_ERR_INVALID_ARG, "gb_jkj_ri_mixed_jr: null pointer");
+  GB_REQUIRE(0 <= q0 && q0 <= q1 && q1 <= P && q0 % SL_ROWS == 0, GB_ERR_BAD_SHAPE,
+             "gb_jkj_ri_mixed_jr: need 0 <= q0 <= q1 <= nbf5 and q0 a multiple of %d (%d, %d, %d)", SL_ROWS, q0, q1,
+             P);
+  Carve pc(const_cast<void*>(prep), gb_ri_prepare_bytes_mixed(N, Q, S));
+  Prepared pr;
+  prepared_layout(pc, N, Q, S, &pr);
+  Carve wc(workspace, workspace_bytes);
+  JkjMixedWs w;
+  jkj_mixed_layout(wc, N, P, Q, S, &w);
+  return jkj_mixed_jr(pr, w, N, P, Q, S, q0, q1, J, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int gb_jkj_ri_mixed_k(int nbf, int nbf5, int naux, int nslices, int q0, int q1, double* K,

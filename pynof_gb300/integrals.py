@@ -116,8 +116,9 @@ def jkj_ri_device(C, b_mnl, nbf5):
 
 def JKj_RI_GPU(C, b_mnl, p):
     """J, K (nbf5, nbf, nbf) -- ``pynof/integrals.py:234-245``.  On the tensor
-    cores the copies to the host overlap the build (J while K is formed, K in
-    two ranges of orbitals)."""
+    cores the copies to the host overlap the build: after T is formed, J and K
+    are formed over alternating ranges of 128 orbitals and each range is
+    copied as soon as it is done."""
     if PRECISION["mode"] == "mixed":
         db = as_device(b_mnl)
         return ops.jkj_ri_mixed_host(as_device(C), prepared(db, PRECISION["nslices"]), p.nbf5)

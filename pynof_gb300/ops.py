@@ -508,16 +508,18 @@ def _copy_stream(dev: torch.device, main: torch.cuda.Stream) -> torch.cuda.Strea
         return s
 
 
-def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int = 2):
+def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, block: int = 128):
     """J, K (nbf5, nbf, nbf) as numpy arrays in pinned host memory, with the
-    device-to-host copies overlapped with the build: J is copied while K is
-    formed, and K in ``parts`` ranges of orbitals, each range as soon as it is
-    done (a second stream; ``gb_jkj_ri_mixed_j`` / ``gb_jkj_ri_mixed_k``).
+    device-to-host copies overlapped with the build.  The build runs as its
+    prelude (T, d: ``gb_jkj_ri_mixed_t``), then J and K over alternating
+    ranges of ``block`` orbitals (a multiple of 128: ``gb_jkj_ri_mixed_jr`` /
+    ``gb_jkj_ri_mixed_k``); each range is copied on a second stream as soon as
+    it is done, so the copies run back to back from shortly after T is formed.
     Bitwise the results of :func:`jkj_ri_mixed`."""
     N, Q, S = prep.nbf, prep.naux, prep.nslices
     _require(C, (N, N), "C")
-    if parts < 1:
-        raise ValueError("parts must be >= 1")
+    if block < 128 or block % 128:
+        raise ValueError("block must be a positive multiple of 128")
     dev = prep.device
     J = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
     K = torch.empty((nbf5, N, N), dtype=_F64, device=dev)
@@ -526,14 +528,14 @@ def jkj_ri_mixed_host(C: torch.Tensor, prep: PreparedRI, nbf5: int, parts: int =
     wp, wn = _ws("gb_jkj_ri_workspace_mixed", N, nbf5, Q, S, device=dev)
     main = torch.cuda.current_stream(dev)
     cs = _copy_stream(dev, main)
-    _lib.call("gb_jkj_ri_mixed_j", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, _ptr(J), wp, wn, main.cuda_stream)
-    cs.wait_stream(main)
-    with torch.cuda.stream(cs):
-        Jh.copy_(J, non_blocking=True)
-    bounds = [nbf5 * i // parts for i in range(parts + 1)]
-    for q0, q1 in zip(bounds[:-1], bounds[1:]):
-        if q1 == q0:
-            continue
+    _lib.call("gb_jkj_ri_mixed_t", _ptr(C), prep.buf.data_ptr(), N, nbf5, Q, S, wp, wn, main.cuda_stream)
+    for q0 in range(0, nbf5, block):
+        q1 = min(q0 + block, nbf5)
+        _lib.call("gb_jkj_ri_mixed_jr", prep.buf.data_ptr(), N, nbf5, Q, S, q0, q1, _ptr(J), wp, wn,
+                  main.cuda_stream)
+        cs.wait_stream(main)
+        with torch.cuda.stream(cs):
+            Jh[q0:q1].copy_(J[q0:q1], non_blocking=True)
         _lib.call("gb_jkj_ri_mixed_k", N, nbf5, Q, S, q0, q1, _ptr(K), wp, wn, main.cuda_stream)
         cs.wait_stream(main)
         with torch.cuda.stream(cs):

@@ -191,21 +191,21 @@ def test_jkh_lagrange2_fused_mixed_golden(case):
         assert nrel(got.cpu().numpy(), g[want]) < 1e-10, want
 
 
-@pytest.mark.parametrize("parts", [1, 2, 3, 7])
-def test_split_build_matches_one_call(torch_cuda, parts):
-    """J and K formed in two C-ABI calls (J, then K over ranges of orbitals),
-    copied to the host on a second stream, equal the one-call build bitwise."""
+@pytest.mark.parametrize("N,P,Q,block", [(96, 40, 180, 128), (170, 150, 340, 128), (300, 290, 120, 256)])
+def test_split_build_matches_one_call(torch_cuda, N, P, Q, block):
+    """J and K formed in parts (the prelude, then J and K over alternating
+    ranges of orbitals), copied to the host on a second stream, equal the
+    one-call build bitwise."""
     from pynof_gb300 import ops
 
-    N, P, Q = 96, 40, 180
-    rng = np.random.default_rng(parts)
+    rng = np.random.default_rng(N)
     b = rng.standard_normal((N, N, Q)) * 0.1
     b = 0.5 * (b + b.transpose(1, 0, 2))
     C, _ = np.linalg.qr(rng.standard_normal((N, N)))
     db, dC = ops.to_device(b), ops.to_device(C)
     prep = ops.PreparedRI(db, 6)
     J, K = ops.jkj_ri_mixed(dC, prep, P)
-    Jh, Kh = ops.jkj_ri_mixed_host(dC, prep, P, parts=parts)
+    Jh, Kh = ops.jkj_ri_mixed_host(dC, prep, P, block=block)
     assert np.array_equal(Jh, J.cpu().numpy())
     assert np.array_equal(Kh, K.cpu().numpy())
 
@@ -220,3 +220,6 @@ def test_split_build_rejects_bad_range(torch_cuda):
         _lib.call("gb_jkj_ri_mixed_k", N, P, Q, 6, 3, P + 1, K.data_ptr(), wp, wn, ops._stream())
     with pytest.raises(_lib.GBError):
         _lib.call("gb_jkj_ri_mixed_k", N, P, Q, 6, 5, 4, K.data_ptr(), wp, wn, ops._stream())
+    prep = ops.PreparedRI(ops.to_device(np.zeros((N, N, Q))), 6)
+    with pytest.raises(_lib.GBError):  # a J range must start on a 128-orbital block
+        _lib.call("gb_jkj_ri_mixed_jr", prep.buf.data_ptr(), N, P, Q, 6, 3, P, K.data_ptr(), wp, wn, ops._stream())
