@@ -18,8 +18,8 @@ Legs of the default run (``--impl ours``):
           host J, K out (pinned), copies inside the timed region;
   roofline  the dominant kernel's algorithmic rate over the launch time the
           library's event profiler recorded inside the timed region;
-  cpu_baseline  the CPU oracle (numpy/OpenBLAS, all host threads) on a
-          bounded sample of orbitals, scaled to builds/s.
+  cpu_baseline  the CPU oracle (numpy/OpenBLAS, all host threads): whole
+          builds at the same configuration (median of --cpu-reps).
 
 ``--impl reference`` times the CPU restatement of PyNOF's JKj_RI (the
 reference itself is Python and is not present at run time) on the same
@@ -664,11 +664,10 @@ def run_precision(args):
     if not args.no_cpu_baseline:
         from oracle import pynof_oracle as orc
 
-        sample = max(2, P // 5)
         orc.jkj_ri(C, b, 2)
         t0 = time.perf_counter()
-        orc.jkj_ri(C, b, sample)
-        t_a1 = (time.perf_counter() - t0) * P / sample
+        orc.jkj_ri(C, b, P)
+        t_a1 = time.perf_counter() - t0
         t0 = time.perf_counter()
         orc.jkh_mo_ri(C, H, b, P)
         t_a3 = time.perf_counter() - t0
@@ -676,8 +675,7 @@ def run_precision(args):
         orc.lagrange2(n, cj.copy(), ck.copy(), C, H, None, b, st)
         t_a5 = time.perf_counter() - t0
         cpu = {"cores": os.cpu_count(), "kind": "port",
-               "sample": f"computeJKj on {sample} of {P} orbitals (scaled), computeJKH_MO and computeLagrange2 "
-                         "whole, one call each",
+               "sample": "computeJKj, computeJKH_MO and computeLagrange2, one whole call each",
                "jk_builds_per_s": 1.0 / t_a1, "jkh_mo_per_s": 1.0 / t_a3, "lagrange2_per_s": 1.0 / t_a5}
     line = {"metric": "precision forms of the RI JK build and Lagrangian vs FP64", "unit": "builds/s",
             "value": out["mixed_s6"]["jk_builds_per_s"], "data": "synthetic",
