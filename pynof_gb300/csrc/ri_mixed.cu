@@ -437,17 +437,19 @@ extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* 
 // ---------------------------------------------------------------------------
 namespace {
 struct Lag2MixedWs {
-  SlicedDesc Aall, Tt, Sx, Sy;
+  SlicedDesc Ap, Tt, Sx, Sy;
   double *Tf, *bMO, *Y, *X, *d, *w, *cjm;
   double* part;  // ns partial exchange products (ns > 1)
-  int ns, kc;    // K splits of the exchange GEMM and K per split
+  double* Z;     // Z[m][b] = sum_(q,l) T[q][m][l] Y[b][q][l]
+  int ns, kc;    // K splits of the exchange GEMM (whole ranges of orbitals q) and K per split
   unsigned int* ctr;  // tile counter of the persistent GEMMs
 };
 
-// K splits of the ck exchange GEMM (M = nbf, N = nbf5, K = nbf5 naux): with
-// few output tiles the long K would run on a few CTAs, so it is cut into
-// ranges of >= 768 that run as a batch; the partial products are summed in a
-// fixed order (deterministic).
+// K splits of the exchange GEMM (M = nbf5, N = nbf, K = nbf5 naux): with few
+// output tiles the long K would run on a few CTAs, so it is cut into ranges
+// of >= 768 that run as a batch; the partial products are summed in a fixed
+// order (deterministic).  Each split covers whole orbitals q (nbf5 divisible
+// by the split count), so its part of T is one strided block.
 int exchange_splits(int N, int P, int Q) {
   const long long tiles = (long long)((N + 127) / 128) * ((P + 127) / 128);
   const long long K = (long long)P * Q;
@@ -455,38 +457,40 @@ int exchange_splits(int N, int P, int Q) {
   long long s = (152 + tiles - 1) / tiles;
   s = s < K / 768 ? s : K / 768;
   s = s < 64 ? s : 64;
-  while (s > 1 && K % s != 0) --s;  // equal ranges: every split reads only its own K
+  while (s > 1 && P % s != 0) --s;  // equal ranges of whole orbitals
   return (int)s;
 }
 
-// elag[a][b] = sum_s part[s][a][b], a < N, b < P (elag row stride N)
-__global__ void sum_splits_kernel(const double* __restrict__ part, int ns, int N, int P, double* __restrict__ elag) {
+// out[r][c] (row stride ld) = sum_s part[s][r][c], r < rows, c < cols
+__global__ void sum_splits_kernel(const double* __restrict__ part, int ns, int rows, int cols,
+                                  double* __restrict__ out, int ld) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)N * P) return;
-  const long long NP = (long long)N * P;
+  if (idx >= (long long)rows * cols) return;
+  const long long RC = (long long)rows * cols;
   double v = 0.0;
-  for (int s = 0; s < ns; ++s) v += part[s * NP + idx];
-  elag[(idx / P) * N + idx % P] = v;
+  for (int s = 0; s < ns; ++s) v += part[s * RC + idx];
+  out[(idx / cols) * ld + idx % cols] = v;
 }
 
 template <class Cv>
 void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
-  SlicedDesc Aall = take_sliced(c, 1, N, N, S);
+  SlicedDesc Ap = take_sliced(c, 1, P, N, S);
   auto* tf = c.template take<double>((size_t)P * N * Q);
   SlicedDesc Tt = take_sliced(c, P, Q, N, S);
-  auto* bmo = c.template take<double>((size_t)N * P * Q);
+  auto* bmo = c.template take<double>((size_t)P * P * Q);
   auto* Y = c.template take<double>((size_t)P * P * Q);
   const int ns = exchange_splits(N, P, Q);
-  const int kc = (int)(((long long)P * Q + ns - 1) / ns);  // K per split
+  const int kc = (P / ns) * Q;  // K per split: P / ns whole orbitals
   SlicedDesc Sx = take_sliced(c, ns, N, kc, S);
   SlicedDesc Sy = take_sliced(c, ns, P, kc, S);
   auto* part = ns > 1 ? c.template take<double>((size_t)ns * N * P) : nullptr;
+  auto* Z = c.template take<double>((size_t)N * P);
   auto* X = c.template take<double>((size_t)N * P);
   auto* d = c.template take<double>((size_t)P * Q);
   auto* wv = c.template take<double>((size_t)P * Q);
   auto* cjm = c.template take<double>((size_t)P * P);
   auto* ctr = c.template take<unsigned int>(1);
-  if (w) *w = Lag2MixedWs{Aall, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, ns, kc, ctr};
+  if (w) *w = Lag2MixedWs{Ap, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, Z, ns, kc, ctr};
 }
 }  // namespace
 
@@ -499,8 +503,17 @@ extern "C" size_t gb_lagrange2_ri_workspace_mixed(int nbf, int nbf5, int naux, i
 namespace {
 // computeLagrange2 on the tensor cores; with J_MO, K_MO, H_core non-null also
 // computeJKH_MO at the same orbitals, from the same transform: bMO[a][q][l] =
-// (aq|l), so d[p] = bMO[p][p], J_MO = d d^T and K_MO[p][q] = sum_l bMO[p][q][l]^2
-// (the first nbf5 rows of bMO), H_core[p] = C_p^T H C_p.
+// (aq|l) for a, q < nbf5, so d[p] = bMO[p][p], J_MO = d d^T and
+// K_MO[p][q] = sum_l bMO[p][q][l]^2, H_core[p] = C_p^T H C_p.
+//
+// The Lagrangian (utils.py:262-382, closed shell) is
+//   elag[a][b] = n_b Hmat[a][b] + sum_k bMO[a][b][k] w[b][k]
+//                - sum_(q,k) ck12[b][q] bMO[a][q][k] bMO[b][q][k]     (b < nbf5)
+// for every a < nbf.  With Y[b][q][k] = ck12[b][q] bMO[b][q][k] (q != b) and
+// -w[b][k] on the diagonal blocks, the last two terms are
+// -sum_(q,k) bMO[a][q][k] Y[b][q][k] = -sum_m C[m][a] Z[m][b] with
+// Z[m][b] = sum_(q,k) T[q][m][k] Y[b][q][k]: the MO transform is needed for
+// a < nbf5 only (Y, d), and the tensor-core GEMM contracts T with Y instead.
 int lagrange2_mixed_body(const double* C, const double* H, const void* prep, const double* n, const double* cj12,
                          const double* ck12, int N, int P, int Q, int nbeta, int nalpha, int S, double* elag,
                          double* Hmat, double* J_MO, double* K_MO, double* H_core, void* workspace,
@@ -512,18 +525,18 @@ int lagrange2_mixed_body(const double* C, const double* H, const void* prep, con
   Lag2MixedWs w;
   lag2_mixed_layout(wc, N, P, Q, S, &w);
 
-  // C^T sliced once for all nbf rows; its first nbf5 rows are the half transform's A
-  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Aall, s));
-  SlicedDesc Ap = w.Aall;
-  Ap.rows = P;
-  GB_TRY(half_transform_gemm(Ap, pr.bT, N, P, Q, w.Tf, w.ctr, s));
+  // C^T rows a < nbf5 (K = m): the half transform's and the MO transform's A
+  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Ap, s));
+  GB_TRY(half_transform_gemm(w.Ap, pr.bT, N, P, Q, w.Tf, w.ctr, s));
   GB_TRY(slice_operand(SliceSrc{w.Tf, (long long)N * Q, lin(1), lin(Q), false}, w.Tt, s));
-  // bMO[a][q][l] (batch q)
+  // bMO[a][q][l], a < nbf5 (batch q): rows l (the output's unit stride, the
+  // persistent form) x orbitals a on the N tile (a ragged orbital count pads
+  // less there)
   OzGemm gm{};
-  gm.M = N; gm.N = Q; gm.K = N; gm.batch = P; gm.S = S;
-  gm.C = w.bMO; gm.c_sb = Q; gm.c_r = lin((long long)P * Q); gm.c_c = lin(1);
+  gm.M = Q; gm.N = P; gm.K = N; gm.batch = P; gm.S = S;
+  gm.C = w.bMO; gm.c_sb = Q; gm.c_r = lin(1); gm.c_c = lin((long long)P * Q);
   gm.sym = SYM_NONE; gm.tag = "ozaki_tc:bMO"; gm.tile_counter = w.ctr;
-  GB_TRY(ozaki_gemm(w.Aall, w.Tt, gm, s));
+  GB_TRY(ozaki_gemm(w.Tt, w.Ap, gm, s));
   GB_TRY(hcore_f64(C, H, N, P, w.X, H_core, Hmat, s));
   GB_TRY(launch_gather_diag(w.bMO, w.d, P, Q, (long long)P * Q + Q, s));
   if (J_MO) {
@@ -551,22 +564,36 @@ int lagrange2_mixed_body(const double* C, const double* H, const void* prep, con
   GB_TRY(launch_add_scaled_rows(w.w, w.d, n, P, Q, nbeta, nalpha, s));
   // the w term rides in the diagonal blocks of the exchange operand
   GB_TRY(launch_make_exchange_operand(w.bMO, ck12, w.w, w.Y, P, Q, s));
-  // elag[a][b] = -sum_(q,l) bMO[a][(q,l)] Y[b][(q,l)], K cut into w.ns equal
-  // ranges (split s = batch s: element (row, k) at row * P Q + s kc + k)
-  GB_TRY(slice_operand(SliceSrc{w.bMO, w.kc, lin((long long)P * Q), lin(1), true}, w.Sx, s));
+  // Z[m][b] = sum_(q,l) T[q][m][l] Y[b][q][l]; K = (q, l) cut into w.ns ranges
+  // of whole orbitals (split s = batch s: its T block starts at orbital
+  // s P / ns, element (m, k) at k / Q * N Q + m Q + k % Q; Y row b at b P Q + s kc + k)
+  const long long qps = P / w.ns;  // orbitals per split
+  GB_TRY(slice_operand(SliceSrc{w.Tf, qps * N * Q, lin(Q), split(Q, (long long)N * Q, 1), true}, w.Sx, s));
   GB_TRY(slice_operand(SliceSrc{w.Y, w.kc, lin((long long)P * Q), lin(1), true}, w.Sy, s));
+  // rows m x orbitals b on the N tile (a ragged orbital count pads less there)
   OzGemm ge{};
   ge.M = N; ge.N = P; ge.K = w.kc; ge.batch = w.ns; ge.S = S;
-  ge.sym = SYM_NONE; ge.negate = 1; ge.tag = "ozaki_tc:ck_exchange"; ge.tile_counter = w.ctr;
+  ge.sym = SYM_NONE; ge.tag = "ozaki_tc:ck_exchange"; ge.tile_counter = w.ctr;
   if (w.ns > 1) {
     ge.C = w.part; ge.c_sb = (long long)N * P; ge.c_r = lin(P); ge.c_c = lin(1);
     GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
     const long long np = (long long)N * P;
-    GB_LAUNCH("sum_splits", s, sum_splits_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(w.part, w.ns, N, P, elag));
+    GB_LAUNCH("sum_splits", s,
+              sum_splits_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(w.part, w.ns, N, P, w.Z, P));
   } else {
-    ge.C = elag; ge.c_sb = 0; ge.c_r = lin(N); ge.c_c = lin(1);
+    ge.C = w.Z; ge.c_sb = 0; ge.c_r = lin(P); ge.c_c = lin(1);
     GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
   }
+  // elag[a][b] = -sum_m C[m][a] Z[m][b] (b < nbf5), then the n_b Hmat term
+  GemmF64 gz{};
+  gz.M = N; gz.N = P; gz.K = N; gz.batch = 1;
+  gz.A = {C, 0, lin(1), lin(N)};
+  gz.B = {w.Z, 0, lin(P), lin(1)};
+  gz.C = {elag, 0, lin(N), lin(1)};
+  gz.alpha = -1.0; gz.beta = 0.0; gz.sym = SYM_NONE;
+  gz.a_kfast = false; gz.b_kfast = false;
+  gz.tag = "gemm_f64:small";
+  GB_TRY(gemm_f64(gz, s));
   return launch_lagrange2_hterm(Hmat, n, elag, N, P, s);
 }
 

@@ -70,9 +70,22 @@ __global__ void rowexp_kfast_kernel(SliceSrc src, int rows, int K, int* __restri
   if (row >= rows) return;
   const double* base = src.p + b * src.sb + src.row_at(row);
   unsigned long long mx = 0;
-  for (int k = lane; k < K; k += 32) {
-    const unsigned long long v = abs_bits(base[src.k.at(k)]);
-    mx = v > mx ? v : mx;
+  if (src.k.div == 0) {
+    for (int k = lane; k < K; k += 32) {
+      const unsigned long long v = abs_bits(base[(long long)k * src.k.s0]);
+      mx = v > mx ? v : mx;
+    }
+  } else {
+    // k runs of length div (stride s0 inside, s1 between runs): no division per element
+    const long long div = src.k.div;
+    for (long long k0 = 0, r = 0; k0 < K; k0 += div, ++r) {
+      const double* bp = base + r * src.k.s1;
+      const long long lim = K - k0 < div ? K - k0 : div;
+      for (long long j = lane; j < lim; j += 32) {
+        const unsigned long long v = abs_bits(bp[j * src.k.s0]);
+        mx = v > mx ? v : mx;
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -118,8 +131,10 @@ constexpr int SL_KPC = 8;
 // The 8 source values of thread (row r, k group at k0) of one k block.
 __device__ __forceinline__ void load_group(const SliceSrc& src, const double* base, bool rok, int k0, int K,
                                            double (&xs)[8]) {
-  const double* p8 = base + k0;
-  if (rok && src.kfast && src.k.div == 0 && src.k.s0 == 1 && k0 + 8 <= K &&
+  // k0 is a multiple of 8: with a unit k stride inside runs of a multiple of 8
+  // (k.div), the 8 values are contiguous
+  const double* p8 = base + src.k.at(k0);
+  if (rok && src.kfast && src.k.s0 == 1 && (src.k.div == 0 || src.k.div % 8 == 0) && k0 + 8 <= K &&
       (reinterpret_cast<uintptr_t>(p8) & 15) == 0) {
     // contiguous, 16-byte aligned k run: four 16-byte loads
 #pragma unroll
