@@ -438,6 +438,7 @@ extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* 
 namespace {
 struct Lag2MixedWs {
   SlicedDesc Ap, Tt, Sx, Sy;
+  SlicedDesc dS, dT, cjS, Ct, Zt;  // the small GEMMs' operands (w, J_MO, elag = -C^T Z)
   double *Tf, *bMO, *Y, *X, *d, *w, *cjm;
   double* part;  // ns partial exchange products (ns > 1)
   double* Z;     // Z[m][b] = sum_(q,l) T[q][m][l] Y[b][q][l]
@@ -490,7 +491,12 @@ void lag2_mixed_layout(Cv& c, int N, int P, int Q, int S, Lag2MixedWs* w) {
   auto* wv = c.template take<double>((size_t)P * Q);
   auto* cjm = c.template take<double>((size_t)P * P);
   auto* ctr = c.template take<unsigned int>(1);
-  if (w) *w = Lag2MixedWs{Ap, Tt, Sx, Sy, tf, bmo, Y, X, d, wv, cjm, part, Z, ns, kc, ctr};
+  SlicedDesc dS = take_sliced(c, 1, P, Q, S);  // d rows p, K = l
+  SlicedDesc dT = take_sliced(c, 1, Q, P, S);  // d^T rows l, K = q
+  SlicedDesc cjS = take_sliced(c, 1, P, P, S);  // cj12 (zero diagonal) rows b, K = q
+  SlicedDesc Ct = take_sliced(c, 1, N, N, S);  // C^T rows a, K = m
+  SlicedDesc Zt = take_sliced(c, 1, P, N, S);  // Z^T rows b, K = m
+  if (w) *w = Lag2MixedWs{Ap, Tt, Sx, Sy, dS, dT, cjS, Ct, Zt, tf, bmo, Y, X, d, wv, cjm, part, Z, ns, kc, ctr};
 }
 }  // namespace
 
@@ -539,28 +545,26 @@ int lagrange2_mixed_body(const double* C, const double* H, const void* prep, con
   GB_TRY(ozaki_gemm(w.Tt, w.Ap, gm, s));
   GB_TRY(hcore_f64(C, H, N, P, w.X, H_core, Hmat, s));
   GB_TRY(launch_gather_diag(w.bMO, w.d, P, Q, (long long)P * Q + Q, s));
+  // d's slices: rows p over K = l (J_MO) and rows l over K = q (w)
+  GB_TRY(slice_operand(SliceSrc{w.d, 0, lin(Q), lin(1), true}, w.dS, s));
+  GB_TRY(slice_operand(SliceSrc{w.d, 0, lin(1), lin(Q), false}, w.dT, s));
   if (J_MO) {
-    GemmF64 gj{};
-    gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1;
-    gj.A = {w.d, 0, lin(Q), lin(1)};
-    gj.B = {w.d, 0, lin(1), lin(Q)};
-    gj.C = {J_MO, 0, lin(P), lin(1)};
-    gj.alpha = 1.0; gj.beta = 0.0; gj.sym = SYM_ROWCOL;
-    gj.a_kfast = true; gj.b_kfast = true;
-    gj.tag = "gemm_f64:small";
-    GB_TRY(gemm_f64(gj, s));
+    // J_MO = d d^T (symmetric: the SYRK form, stored transposed)
+    OzGemm gj{};
+    gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1; gj.S = S;
+    gj.C = J_MO; gj.c_sb = 0; gj.c_r = lin(1); gj.c_c = lin(P);
+    gj.sym = SYM_ROWCOL; gj.tag = "ozaki_tc:J_MO"; gj.tile_counter = w.ctr;
+    GB_TRY(ozaki_gemm(w.dS, w.dS, gj, s));
     GB_TRY(launch_row_sumsq(w.bMO, K_MO, (long long)P * P, Q, s));
   }
+  // w[b][l] = sum_q cj12[b][q] d[q][l] (diagonal of cj12 zero): rows l x orbitals b
   GB_TRY(launch_copy_zero_diag(cj12, w.cjm, P, s));
-  GemmF64 gw{};
-  gw.M = P; gw.N = Q; gw.K = P; gw.batch = 1;
-  gw.A = {w.cjm, 0, lin(P), lin(1)};
-  gw.B = {w.d, 0, lin(Q), lin(1)};
-  gw.C = {w.w, 0, lin(Q), lin(1)};
-  gw.alpha = 1.0; gw.beta = 0.0; gw.sym = SYM_NONE;
-  gw.a_kfast = true; gw.b_kfast = false;
-  gw.tag = "gemm_f64:small";
-  GB_TRY(gemm_f64(gw, s));
+  GB_TRY(slice_operand(SliceSrc{w.cjm, 0, lin(P), lin(1), true}, w.cjS, s));
+  OzGemm gw{};
+  gw.M = Q; gw.N = P; gw.K = P; gw.batch = 1; gw.S = S;
+  gw.C = w.w; gw.c_sb = 0; gw.c_r = lin(1); gw.c_c = lin(Q);
+  gw.sym = SYM_NONE; gw.tag = "ozaki_tc:w"; gw.tile_counter = w.ctr;
+  GB_TRY(ozaki_gemm(w.dT, w.cjS, gw, s));
   GB_TRY(launch_add_scaled_rows(w.w, w.d, n, P, Q, nbeta, nalpha, s));
   // the w term rides in the diagonal blocks of the exchange operand
   GB_TRY(launch_make_exchange_operand(w.bMO, ck12, w.w, w.Y, P, Q, s));
@@ -585,15 +589,13 @@ int lagrange2_mixed_body(const double* C, const double* H, const void* prep, con
     GB_TRY(ozaki_gemm(w.Sx, w.Sy, ge, s));
   }
   // elag[a][b] = -sum_m C[m][a] Z[m][b] (b < nbf5), then the n_b Hmat term
-  GemmF64 gz{};
-  gz.M = N; gz.N = P; gz.K = N; gz.batch = 1;
-  gz.A = {C, 0, lin(1), lin(N)};
-  gz.B = {w.Z, 0, lin(P), lin(1)};
-  gz.C = {elag, 0, lin(N), lin(1)};
-  gz.alpha = -1.0; gz.beta = 0.0; gz.sym = SYM_NONE;
-  gz.a_kfast = false; gz.b_kfast = false;
-  gz.tag = "gemm_f64:small";
-  GB_TRY(gemm_f64(gz, s));
+  GB_TRY(slice_operand(SliceSrc{C, 0, lin(1), lin(N), false}, w.Ct, s));
+  GB_TRY(slice_operand(SliceSrc{w.Z, 0, lin(1), lin(P), false}, w.Zt, s));
+  OzGemm gz{};
+  gz.M = N; gz.N = P; gz.K = N; gz.batch = 1; gz.S = S; gz.negate = 1;
+  gz.C = elag; gz.c_sb = 0; gz.c_r = lin(N); gz.c_c = lin(1);
+  gz.sym = SYM_NONE; gz.tag = "ozaki_tc:elag"; gz.tile_counter = w.ctr;
+  GB_TRY(ozaki_gemm(w.Ct, w.Zt, gz, s));
   return launch_lagrange2_hterm(Hmat, n, elag, N, P, s);
 }
 
