@@ -333,7 +333,7 @@ extern "C" int gb_dgemm_mixed(const double* A, const double* B, int M, int N, in
 // ---------------------------------------------------------------------------
 namespace {
 struct JkhMixedWs {
-  SlicedDesc A, Tt;
+  SlicedDesc A, Tt, dS;
   double *Tf, *bpq, *d, *X;
   unsigned int* ctr;  // tile counter of the persistent GEMMs
 };
@@ -347,7 +347,8 @@ void jkh_mixed_layout(Cv& c, int N, int P, int Q, int S, JkhMixedWs* w) {
   auto* d = c.template take<double>((size_t)P * Q);
   auto* X = c.template take<double>((size_t)N * P);
   auto* ctr = c.template take<unsigned int>(1);
-  if (w) *w = JkhMixedWs{A, Tt, tf, bpq, d, X, ctr};
+  SlicedDesc dS = take_sliced(c, 1, P, Q, S);  // d rows p, K = l (J_MO)
+  if (w) *w = JkhMixedWs{A, Tt, dS, tf, bpq, d, X, ctr};
 }
 
 // H_core[p] = C_p^T H C_p and (optionally) Hmat = C^T H C_p in FP64
@@ -416,15 +417,13 @@ extern "C" int gb_jkh_mo_ri_mixed(const double* C, const double* H, const void* 
     GB_TRY(ozaki_gemm(w.A, w.Tt, gq, s));
   }
   GB_TRY(launch_gather_diag(w.bpq, w.d, P, Q, (long long)P * Q + Q, s));
-  GemmF64 gj{};
-  gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1;
-  gj.A = {w.d, 0, lin(Q), lin(1)};
-  gj.B = {w.d, 0, lin(1), lin(Q)};
-  gj.C = {J_MO, 0, lin(P), lin(1)};
-  gj.alpha = 1.0; gj.beta = 0.0; gj.sym = SYM_ROWCOL;
-  gj.a_kfast = true; gj.b_kfast = true;
-  gj.tag = "gemm_f64:small";
-  GB_TRY(gemm_f64(gj, s));
+  // J_MO = d d^T (symmetric: the SYRK form, stored transposed)
+  GB_TRY(slice_operand(SliceSrc{w.d, 0, lin(Q), lin(1), true}, w.dS, s));
+  OzGemm gj{};
+  gj.M = P; gj.N = P; gj.K = Q; gj.batch = 1; gj.S = S;
+  gj.C = J_MO; gj.c_sb = 0; gj.c_r = lin(1); gj.c_c = lin(P);
+  gj.sym = SYM_ROWCOL; gj.tag = "ozaki_tc:J_MO"; gj.tile_counter = w.ctr;
+  GB_TRY(ozaki_gemm(w.dS, w.dS, gj, s));
   GB_TRY(launch_row_sumsq(w.bpq, K_MO, (long long)P * P, Q, s));
   return hcore_f64(C, H, N, P, w.X, H_core, nullptr, s);
 }
