@@ -253,6 +253,41 @@ int gb_occ_energy_grad_f64(const double* gamma, const double* J_MO, const double
 int gb_calce_f64(const double* n, const double* cj12, const double* ck12, const double* J_MO, const double* K_MO,
                  const double* H_core, int nbf5, int nbeta, int nalpha, double* energy);
 
+/* A9  occoptr's minimisation (pynof/minimization.py:77-97:
+ * scipy.optimize.minimize(calcocce, gamma, jac=calcoccg, method="CG")) on the
+ * DEVICE, with every argument pointer in device memory: J_MO, K_MO
+ * [nbf5][nbf5], H_core [nbf5], gamma0 [ndoc ncwo] (closed shell, nsoc = 0,
+ * no1 + ndoc (1 + ncwo) <= nbf5).  The energy and gradient are those of
+ * gb_occ_energy_grad_f64 (softmax occupations, CJCKD8 and its derivative,
+ * pnof.py:350-525, 770-809, 994-1033); the minimiser is scipy's CG
+ * (Polak-Ribiere+ with the sufficient-descent check, More-Thuente line search
+ * with c1 = 1e-4, c2 = 0.4), stopping at ||g||_inf <= gtol (scipy's 1e-5) or
+ * after maxiter iterations (scipy's 200 ndoc ncwo).  Where scipy would try its
+ * second line search it restarts from steepest descent once, then stops.
+ * The whole loop is one CUDA graph on `stream` (a WHILE conditional node; no
+ * host synchronisation): result[5] = {E, iterations, evaluations, success
+ * (1, 0, or -1 when the evaluation cap 1 + 200 (maxiter + 1) was reached),
+ * ||g||_inf}, gamma_out [ndoc ncwo] (may alias gamma0), and, when not null,
+ * the occupations n_out [nbf5] (ocupacion_softmax) and C^J, C^K
+ * [nbf5][nbf5] (CJCKD8, diagonals included) at the result.  `ws` is
+ * 256-byte-aligned device memory of gb_occ_workspace_bytes bytes; one
+ * minimisation at a time per workspace (the graph is cached per workspace
+ * and context; gb_occ_release drops it).  Not capturable into another
+ * graph. */
+size_t gb_occ_workspace_bytes(int nbf5, int ndoc, int ncwo);
+int gb_occ_minimize_dev(const double* gamma0, const double* J_MO, const double* K_MO, const double* H_core,
+                        int nbf5, int no1, int ndoc, int ncwo, double gtol, int maxiter, double* gamma_out,
+                        double* result, double* n_out, double* cj12_out, double* ck12_out, void* ws,
+                        size_t ws_bytes, void* stream);
+/* One evaluation of E(gamma) and dE/dgamma on the device (calcocce +
+ * calcoccg, pnof.py:994-1033): result[0] = E, result[4] = ||g||_inf, grad
+ * [ndoc ncwo] (may be null); same workspace as gb_occ_minimize_dev. */
+int gb_occ_energy_grad_dev(const double* gamma, const double* J_MO, const double* K_MO, const double* H_core,
+                           int nbf5, int no1, int ndoc, int ncwo, double* result, double* grad, void* ws,
+                           size_t ws_bytes, void* stream);
+/* Drop the cached graph of a workspace (before freeing it). */
+int gb_occ_release(const void* ws);
+
 /* Plain FP64 GEMM C = A B^T with row-major A [M][K], B [N][K], C [M][N] on the
  * DMMA engine (the FP64 counterpart of gb_dgemm_mixed).  No counterpart in
  * the reference (numpy / cupy GEMMs); used e.g. for ERPA's (pq|sl) from b_pql

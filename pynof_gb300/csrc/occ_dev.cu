@@ -1,0 +1,981 @@
+// Occupation optimiser on the device: E(gamma), dE/dgamma and the whole
+// conjugate-gradient minimisation over gamma at fixed J_MO, K_MO, H_core
+// (occoptr, minimization.py:77-97, which calls scipy's CG on calcocce /
+// calcoccg), without a host round trip per evaluation.
+//
+// One evaluation at a trial point gamma_t:
+//  - occupations from the softmax parameterisation (ocupacion_softmax,
+//    pnof.py:770-809; the strong occupation of pair i written at index i as
+//    the reference does) and the per-orbital GNOF quantities of CJCKD8
+//    (pnof.py:350-422): n, nd = n F(n_s), sqrt(nd), fi = sqrt(n (1 - n)) and
+//    its derivative;
+//  - the pair sums over (a, b) from different pairs (calce, pnof.py:905-929,
+//    and the gradient of calcoccg, pnof.py:1004-1033 with der_CJCKD8,
+//    pnof.py:425-525): occ_rows_kernel, one warp per (32 orbitals a, 16
+//    orbitals b) item on a fixed grid, lanes over a so that J[b][a] and
+//    K[b][a] are read coalesced; per a: the energy terms in a compensated
+//    (Neumaier) sum, the dE/dn term and the two sums that give dE/dnd;
+//  - occ_reduce_kernel: one warp per a over its b chunks (fixed tree order);
+//  - occ_step_kernel (one CTA): the diagonal and same-pair terms, the chain
+//    rule through nd = n F(n_s), g = dn^T e, and the energy -- the same
+//    assembly as the host loop of occ_host.cu.
+//
+// The minimiser is scipy's CG as scipy 1.18 runs it: Polak-Ribiere+ with the
+// sufficient-descent check, the first trial step from the previous decrease,
+// and the line search of More & Thuente (ACM TOMS 20 (1994) 286-307; strong
+// Wolfe with c1 = 1e-4, c2 = 0.4, xtol 1e-14, steps in [1e-100, 1e100], at most
+// 100 calls), as a state machine that occ_step_kernel advances by one
+// evaluation.  Where scipy would try its second line search (a failed search,
+// or a step without sufficient descent), the state machine restarts from
+// steepest descent once and otherwise stops at the current point.
+//
+// One CUDA graph per workspace runs a whole minimisation: an init kernel, a
+// WHILE conditional node whose body is rows -> reduce -> step (the step kernel
+// clears the condition when the minimiser stops), then the occupations and
+// C^J, C^K at the result.  The number of evaluations is capped at
+// 1 + 200 (maxiter + 1): a minimiser that reaches the cap reports success -1.
+//
+// All arithmetic is FP64 (GB300's FP64 rate is low, so the O(nbf5^2) pair
+// work is spread over the whole GPU and the single-CTA work is O(nbf5)).
+// Closed shell without singly occupied orbitals (MSpin = 0, nsoc = 0).
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr int kStepThreads = 256;
+constexpr int kRowCtas = 4 * 152;  // rows kernel: one warp per CTA, grid-stride over items
+constexpr int kRedCtas = 2 * 152;  // reduce kernel: one warp per CTA
+constexpr int kCjckCtas = 2 * 152;
+constexpr int kBch = 16;           // orbitals b per item of the rows kernel
+constexpr double kHCut = 0.02 * 1.4142135623730951;
+// line search constants
+constexpr double kFtol = 1e-4, kGtol = 0.4, kXtol = 1e-14, kStpMin = 1e-100, kStpMax = 1e100;
+constexpr double kXtrapL = 1.1, kXtrapU = 4.0, kP5 = 0.5, kP66 = 0.66;
+constexpr int kMaxCalls = 100;
+
+enum { MODE_MIN = 0, MODE_EVAL = 1 };
+enum { PH_INIT = 0, PH_LS = 1, PH_DONE = 2 };
+enum { T_FG = 0, T_CONV = 1, T_FAIL = 2 };
+
+struct OccArgs {
+  const double *J, *K, *H, *gamma0;
+  double *gamma_out, *grad_out, *res, *n_out, *cj_out, *ck_out;
+  // workspace arrays
+  double *x, *g, *p, *pn, *xt, *gt;             // nv
+  double *n, *nd, *nd12, *fi, *fid, *sq, *rsq;  // P
+  double *e, *en;                               // P
+  double *ns, *F, *dF;                          // ndoc
+  double *nw;                                   // nv
+  double *part;                                 // 5 P nbc
+  double *row;                                  // 5 P
+  int *pair_of, *cls;                           // P
+  int P, no1, ndoc, ncwo, nv, nbc, maxiter, mode;
+  double gtol;
+};
+
+struct OccState {
+  OccArgs a;
+  // conjugate gradients
+  double f, f_prev, gnorm, delta;
+  int k, nev, maxev, phase, restarted;
+  // More-Thuente line search
+  double stp, finit, ginit, gtest, width, width1, stx, fx, gx, sty, fy, gy, stmin, stmax;
+  int brackt, stage, calls;
+};
+
+__device__ __forceinline__ int weak_of(const OccArgs& a, int p, int j) {
+  return a.no1 + a.ndoc + (a.ndoc - p - 1) + a.ndoc * j;
+}
+__device__ __forceinline__ int gam_of(const OccArgs& a, int p, int j) { return (a.ndoc - p - 1) + a.ndoc * j; }
+
+// Neumaier's compensated addition (A. Neumaier, ZAMM 54 (1974) 39-51).
+__device__ __forceinline__ void comp_add(double& s, double& c, double x) {
+  const double t = s + x;
+  c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
+// NaN-propagating maximum of |v| (numpy's max of abs)
+__device__ __forceinline__ double nanmax(double a, double b) { return (a > b || a != a) ? a : b; }
+
+// ---- deterministic block reductions (fixed tree; every thread gets the value)
+__device__ double block_sum(double v, double* sh) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = l < kStepThreads / 32 ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (l == 0) sh[32] = v;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+__device__ double block_max(double v, double* sh) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = l < kStepThreads / 32 ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (l == 0) sh[32] = v;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+__device__ double block_comp(double s, double c, double* sh) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+    if (l + o < 32) {
+      comp_add(s, c, s2);
+      comp_add(s, c, c2);
+    }
+  }
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = s;
+    sh[8 + w] = c;
+  }
+  __syncthreads();
+  if (w == 0) {
+    s = l < kStepThreads / 32 ? sh[l] : 0.0;
+    c = l < kStepThreads / 32 ? sh[8 + l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+      if (l + o < 32) {
+        comp_add(s, c, s2);
+        comp_add(s, c, c2);
+      }
+    }
+    if (l == 0) sh[32] = s + c;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+// ---- the trial point's per-orbital quantities (all threads of one CTA)
+__device__ void prep_point(const OccArgs& a, const double* __restrict__ x) {
+  const int tid = threadIdx.x;
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    double top = -INFINITY, den = 1.0;
+    for (int j = 0; j < a.ncwo; ++j) top = fmax(top, x[gam_of(a, p, j)]);
+    double ns;
+    if (top >= 700.0) {
+      // logits past exp's range: the same softmax shifted by the largest one
+      den = exp(-top);
+      for (int j = 0; j < a.ncwo; ++j) den += exp(x[gam_of(a, p, j)] - top);
+      ns = exp(-top) / den;
+      for (int j = 0; j < a.ncwo; ++j) a.nw[p * a.ncwo + j] = exp(x[gam_of(a, p, j)] - top) / den;
+    } else {
+      for (int j = 0; j < a.ncwo; ++j) den += exp(fmin(x[gam_of(a, p, j)], 700.0));
+      ns = 1.0 / den;
+      for (int j = 0; j < a.ncwo; ++j) a.nw[p * a.ncwo + j] = exp(fmin(x[gam_of(a, p, j)], 700.0)) / den;
+    }
+    a.ns[p] = ns;
+    a.n[p] = ns;
+    for (int j = 0; j < a.ncwo; ++j) a.n[weak_of(a, p, j)] = a.nw[p * a.ncwo + j];
+  }
+  __syncthreads();
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    const int s = a.no1 + p;
+    const double coc = (1.0 - a.n[s]) / kHCut;
+    const double F = exp(-coc * coc);
+    a.F[p] = F;
+    a.dF[p] = 2.0 * coc / kHCut;  // (1/F) dF/dn_s
+    a.nd[s] = a.n[s] * F;
+    for (int j = 0; j < a.ncwo; ++j) {
+      const int w = weak_of(a, p, j);
+      a.nd[w] = a.n[w] * F;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < a.P; i += kStepThreads) {
+    const double ni = a.n[i];
+    const double fi = sqrt(fmax(ni * (1.0 - ni), 0.0));
+    a.nd12[i] = sqrt(a.nd[i]);
+    a.fi[i] = fi;
+    a.fid[i] = i < a.no1 ? 0.0 : (1.0 - 2.0 * ni) / (2.0 * fmax(fi, 1e-15));
+    a.sq[i] = sqrt(ni);
+    a.rsq[i] = 1.0 / sqrt(fmax(ni, 1e-15));
+  }
+  __syncthreads();
+}
+
+// ---- pair sums over b for 32 orbitals a
+__global__ void __launch_bounds__(32) occ_rows_kernel(const OccState* __restrict__ st) {
+  const OccArgs& a = st->a;
+  if (st->phase == PH_DONE) return;
+  const int P = a.P, nbc = a.nbc, lane = threadIdx.x;
+  const int nag = (P + 31) / 32;
+  for (int it = blockIdx.x; it < nag * nbc; it += gridDim.x) {
+    const int ag = it / nbc, bc = it - ag * nbc;
+    const int i = ag * 32 + lane;
+    if (i >= P) continue;
+    const int pa = a.pair_of[i], ca = a.cls[i];
+    const double ni = a.n[i], fii = a.fi[i], fidi = a.fid[i], nd12i = a.nd12[i], ndi = a.nd[i];
+    double Es = 0.0, Ec = 0.0, ea = 0.0, S1 = 0.0, S2 = 0.0;
+    const int b0 = bc * kBch, b1 = min(P, b0 + kBch);
+    for (int b = b0; b < b1; ++b) {
+      if (b == i || (pa >= 0 && a.pair_of[b] == pa)) continue;
+      const double Jba = a.J[(size_t)b * P + i], Kba = a.K[(size_t)b * P + i];
+      const double nb = a.n[b];
+      const int cb = a.cls[b];
+      ea += 4.0 * nb * Jba;
+      double ck = ni * nb, dck = nb;
+      if ((ca == 1 && cb == 2) || (ca == 2 && cb >= 1)) {
+        const double sg = (ca == 2 && cb == 2) ? -1.0 : 1.0;
+        ck += fii * a.fi[b] + sg * nd12i * a.nd12[b] - ndi * a.nd[b];
+        dck += fidi * a.fi[b];
+        S1 += sg * a.nd12[b] * Kba;
+        S2 += a.nd[b] * Kba;
+      }
+      comp_add(Es, Ec, 2.0 * ni * nb * Jba - ck * Kba);
+      ea -= 2.0 * dck * Kba;
+    }
+    double* q = a.part + (size_t)i * nbc + bc;
+    const size_t plane = (size_t)P * nbc;
+    q[0] = Es;
+    q[plane] = Ec;
+    q[2 * plane] = ea;
+    q[3 * plane] = S1;
+    q[4 * plane] = S2;
+  }
+}
+
+// ---- per orbital a: its b chunks in a fixed tree order
+__global__ void __launch_bounds__(32) occ_reduce_kernel(const OccState* __restrict__ st) {
+  const OccArgs& a = st->a;
+  if (st->phase == PH_DONE) return;
+  const int P = a.P, nbc = a.nbc, l = threadIdx.x;
+  const size_t plane = (size_t)P * nbc;
+  for (int i = blockIdx.x; i < P; i += gridDim.x) {
+    const double* q = a.part + (size_t)i * nbc;
+    double s = 0.0, c = 0.0, ea = 0.0, S1 = 0.0, S2 = 0.0;
+    for (int bc = l; bc < nbc; bc += 32) {
+      comp_add(s, c, q[bc]);
+      comp_add(s, c, q[plane + bc]);
+      ea += q[2 * plane + bc];
+      S1 += q[3 * plane + bc];
+      S2 += q[4 * plane + bc];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+      const double e2 = __shfl_down_sync(0xffffffffu, ea, o), x2 = __shfl_down_sync(0xffffffffu, S1, o),
+                   y2 = __shfl_down_sync(0xffffffffu, S2, o);
+      if (l + o < 32) {
+        comp_add(s, c, s2);
+        comp_add(s, c, c2);
+        ea += e2;
+        S1 += x2;
+        S2 += y2;
+      }
+    }
+    if (l == 0) {
+      a.row[i] = s;
+      a.row[P + i] = c;
+      a.row[2 * P + i] = ea;
+      a.row[3 * P + i] = S1;
+      a.row[4 * P + i] = S2;
+    }
+  }
+}
+
+// ---- energy and gradient at the trial point from the reduced rows (one CTA)
+__device__ double assemble(const OccArgs& a, double* sh) {
+  const int P = a.P, tid = threadIdx.x;
+  double es = 0.0, ec = 0.0;
+  for (int i = tid; i < P; i += kStepThreads) {
+    const double d = 2.0 * a.H[i] + a.J[(size_t)i * P + i];
+    comp_add(es, ec, a.n[i] * d);
+    comp_add(es, ec, a.row[i]);
+    comp_add(es, ec, a.row[P + i]);
+    a.e[i] = d + a.row[2 * P + i];
+    a.en[i] = -2.0 * (a.row[3 * P + i] / (2.0 * fmax(a.nd12[i], 1e-15)) - a.row[4 * P + i]);
+  }
+  __syncthreads();
+  // pairs inside one pair block: C^J = 0; C^K = sqrt(n_s n_w) (strong-weak),
+  // -sqrt(n_w n_w') (weak-weak)
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    const int s = a.no1 + p;
+    double e_s = a.e[s];
+    for (int j = 0; j < a.ncwo; ++j) {
+      const int w = weak_of(a, p, j);
+      const double Kws = a.K[(size_t)w * P + s], Ksw = a.K[(size_t)s * P + w];
+      comp_add(es, ec, -(a.sq[s] * a.sq[w]) * (Kws + Ksw));
+      e_s -= a.sq[w] * a.rsq[s] * Kws;
+      double e_w = a.e[w] - a.sq[s] * a.rsq[w] * Ksw;
+      for (int j2 = 0; j2 < a.ncwo; ++j2) {
+        if (j2 == j) continue;
+        const int w2 = weak_of(a, p, j2);
+        const double Kw2w = a.K[(size_t)w2 * P + w];
+        comp_add(es, ec, a.sq[w] * a.sq[w2] * Kw2w);
+        e_w += a.sq[w2] * a.rsq[w] * Kw2w;
+      }
+      a.e[w] = e_w;
+    }
+    a.e[s] = e_s;
+  }
+  __syncthreads();
+  // nd_s = n_s F(n_s), nd_w = n_w F(n_s): chain dE/dnd to the occupations
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    const int s = a.no1 + p;
+    const double F = a.F[p], dF = a.dF[p];
+    double e_s = a.e[s] + a.en[s] * F * (1.0 + a.n[s] * dF);
+    for (int j = 0; j < a.ncwo; ++j) {
+      const int w = weak_of(a, p, j);
+      a.e[w] += a.en[w] * F;
+      e_s += a.en[w] * a.n[w] * F * dF;
+    }
+    a.e[s] = e_s;
+  }
+  __syncthreads();
+  // g = dn^T e (row p of dn holds the strong occupation)
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    double wsum = 0.0;
+    for (int i = 0; i < a.ncwo; ++i) wsum += a.nw[p * a.ncwo + i] * a.e[weak_of(a, p, i)];
+    for (int j = 0; j < a.ncwo; ++j) {
+      const double w = a.nw[p * a.ncwo + j];
+      a.gt[gam_of(a, p, j)] = -a.ns[p] * w * a.e[p] + w * a.e[weak_of(a, p, j)] - w * wsum;
+    }
+  }
+  return block_comp(es, ec, sh);  // synchronises
+}
+
+// ---- More & Thuente, one safeguarded step (section 4 of the paper)
+__device__ void dcstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy, double& stp,
+                       double fp, double dp, int& brackt, double stpmin, double stpmax) {
+  const double sgnd = dp * (dx / fabs(dx));
+  double stpf;
+  if (fp > fx) {
+    const double theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+    const double s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+    double gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp < stx) gamma = -gamma;
+    const double p = (gamma - dx) + theta;
+    const double q = ((gamma - dx) + gamma) + dp;
+    const double r = p / q;
+    const double stpc = stx + r * (stp - stx);
+    const double stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2.0) * (stp - stx);
+    stpf = fabs(stpc - stx) < fabs(stpq - stx) ? stpc : stpc + (stpq - stpc) / 2.0;
+    brackt = 1;
+  } else if (sgnd < 0.0) {
+    const double theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+    const double s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+    double gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp > stx) gamma = -gamma;
+    const double p = (gamma - dp) + theta;
+    const double q = ((gamma - dp) + gamma) + dx;
+    const double r = p / q;
+    const double stpc = stp + r * (stx - stp);
+    const double stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    stpf = fabs(stpc - stp) > fabs(stpq - stp) ? stpc : stpq;
+    brackt = 1;
+  } else if (fabs(dp) < fabs(dx)) {
+    const double theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+    const double s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+    const double disc = (theta / s) * (theta / s) - (dx / s) * (dp / s);
+    double gamma = s * sqrt(disc > 0.0 ? disc : 0.0);
+    if (stp > stx) gamma = -gamma;
+    const double p = (gamma - dp) + theta;
+    const double q = (gamma + (dx - dp)) + gamma;
+    const double r = p / q;
+    double stpc;
+    if (r < 0.0 && gamma != 0.0)
+      stpc = stp + r * (stx - stp);
+    else if (stp > stx)
+      stpc = stpmax;
+    else
+      stpc = stpmin;
+    const double stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    if (brackt) {
+      stpf = fabs(stpc - stp) < fabs(stpq - stp) ? stpc : stpq;
+      if (stp > stx)
+        stpf = fmin(stp + kP66 * (sty - stp), stpf);
+      else
+        stpf = fmax(stp + kP66 * (sty - stp), stpf);
+    } else {
+      stpf = fabs(stpc - stp) > fabs(stpq - stp) ? stpc : stpq;
+      stpf = fmin(stpmax, stpf);
+      stpf = fmax(stpmin, stpf);
+    }
+  } else {
+    if (brackt) {
+      const double theta = 3.0 * (fp - fy) / (sty - stp) + dy + dp;
+      const double s = fmax(fmax(fabs(theta), fabs(dy)), fabs(dp));
+      double gamma = s * sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+      if (stp > sty) gamma = -gamma;
+      const double p = (gamma - dp) + theta;
+      const double q = ((gamma - dp) + gamma) + dy;
+      const double r = p / q;
+      stpf = stp + r * (sty - stp);
+    } else if (stp > stx) {
+      stpf = stpmax;
+    } else {
+      stpf = stpmin;
+    }
+  }
+  if (fp > fx) {
+    sty = stp;
+    fy = fp;
+    dy = dp;
+  } else {
+    if (sgnd < 0.0) {
+      sty = stx;
+      fy = fx;
+      dy = dx;
+    }
+    stx = stp;
+    fx = fp;
+    dx = dp;
+  }
+  stp = stpf;
+}
+
+__device__ int ls_fg(OccState& S, double stp) {
+  if (!isfinite(stp) || S.calls >= kMaxCalls) return T_FAIL;
+  S.stp = stp;
+  return T_FG;
+}
+
+__device__ int ls_start(OccState& S, double stp, double f, double g) {
+  S.calls = 1;
+  if (stp < kStpMin || stp > kStpMax || g >= 0.0) return T_FAIL;
+  S.brackt = 0;
+  S.stage = 1;
+  S.finit = f;
+  S.ginit = g;
+  S.gtest = kFtol * g;
+  S.width = kStpMax - kStpMin;
+  S.width1 = S.width / kP5;
+  S.stx = 0.0;
+  S.fx = f;
+  S.gx = g;
+  S.sty = 0.0;
+  S.fy = f;
+  S.gy = g;
+  S.stmin = 0.0;
+  S.stmax = stp + kXtrapU * stp;
+  return ls_fg(S, stp);
+}
+
+__device__ int ls_step(OccState& S, double f, double g) {
+  S.calls += 1;
+  double stp = S.stp;
+  const double ftest = S.finit + stp * S.gtest;
+  if (S.stage == 1 && f <= ftest && g >= 0.0) S.stage = 2;
+  const bool warn = (S.brackt && (stp <= S.stmin || stp >= S.stmax)) ||
+                    (S.brackt && S.stmax - S.stmin <= kXtol * S.stmax) ||
+                    (stp == kStpMax && f <= ftest && g <= S.gtest) ||
+                    (stp == kStpMin && (f > ftest || g >= S.gtest));
+  if (f <= ftest && fabs(g) <= kGtol * (-S.ginit)) return T_CONV;
+  if (warn) return T_FAIL;
+  if (S.stage == 1 && f <= S.fx && f > ftest) {
+    // the modified function psi(a) = phi(a) - phi(0) - ftol phi'(0) a
+    double fxm = S.fx - S.stx * S.gtest, fym = S.fy - S.sty * S.gtest;
+    double gxm = S.gx - S.gtest, gym = S.gy - S.gtest;
+    dcstep(S.stx, fxm, gxm, S.sty, fym, gym, stp, f - stp * S.gtest, g - S.gtest, S.brackt, S.stmin, S.stmax);
+    S.fx = fxm + S.stx * S.gtest;
+    S.fy = fym + S.sty * S.gtest;
+    S.gx = gxm + S.gtest;
+    S.gy = gym + S.gtest;
+  } else {
+    dcstep(S.stx, S.fx, S.gx, S.sty, S.fy, S.gy, stp, f, g, S.brackt, S.stmin, S.stmax);
+  }
+  if (S.brackt) {
+    if (fabs(S.sty - S.stx) >= kP66 * S.width1) stp = S.stx + kP5 * (S.sty - S.stx);
+    S.width1 = S.width;
+    S.width = fabs(S.sty - S.stx);
+    S.stmin = fmin(S.stx, S.sty);
+    S.stmax = fmax(S.stx, S.sty);
+  } else {
+    S.stmin = stp + kXtrapL * (stp - S.stx);
+    S.stmax = stp + kXtrapU * (stp - S.stx);
+  }
+  stp = fmin(fmax(stp, kStpMin), kStpMax);
+  if ((S.brackt && (stp <= S.stmin || stp >= S.stmax)) || (S.brackt && S.stmax - S.stmin <= kXtol * S.stmax))
+    stp = S.stx;
+  return ls_fg(S, stp);
+}
+
+// ---- kernels
+__global__ void __launch_bounds__(kStepThreads) occ_init_kernel(OccState* st, OccArgs args) {
+  OccState& S = *st;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    S.a = args;
+    S.phase = PH_INIT;
+    S.nev = 0;
+    S.k = 0;
+    S.restarted = 0;
+    S.maxev = 1 + 200 * (args.maxiter + 1);
+  }
+  const OccArgs& a = args;
+  const int nb = a.no1 + a.ndoc;
+  for (int i = tid; i < a.P; i += kStepThreads) {
+    a.n[i] = 0.0;
+    a.nd[i] = 0.0;
+    a.pair_of[i] = -1;
+    a.cls[i] = i < a.no1 ? 0 : (i < nb ? 1 : 2);  // 1: strong set S, 2: weak set W
+  }
+  __syncthreads();
+  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+    a.pair_of[a.no1 + p] = p;
+    for (int j = 0; j < a.ncwo; ++j) a.pair_of[weak_of(a, p, j)] = p;
+  }
+  for (int i = tid; i < a.nv; i += kStepThreads) {
+    a.x[i] = a.gamma0[i];
+    a.xt[i] = a.gamma0[i];
+  }
+  __syncthreads();
+  prep_point(a, a.xt);
+}
+
+__device__ void finish(OccState& S, double success, cudaGraphConditionalHandle h) {
+  const OccArgs& a = S.a;
+  for (int i = threadIdx.x; i < a.nv; i += kStepThreads) a.gamma_out[i] = a.x[i];
+  if (threadIdx.x == 0) {
+    a.res[0] = S.f;
+    a.res[1] = S.k;
+    a.res[2] = S.nev;
+    a.res[3] = success;
+    a.res[4] = S.gnorm;
+    S.phase = PH_DONE;
+    cudaGraphSetConditional(h, 0);
+  }
+}
+
+__global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h) {
+  __shared__ double sh[40];
+  __shared__ int s_act;
+  OccState& S = *st;
+  const OccArgs& a = S.a;
+  const int tid = threadIdx.x;
+  if (S.phase == PH_DONE) {
+    if (tid == 0) cudaGraphSetConditional(h, 0);
+    return;
+  }
+  const double E = assemble(a, sh);
+  if (tid == 0) S.nev += 1;
+  if (a.mode == MODE_EVAL) {
+    const double gm = [&] {
+      double m = 0.0;
+      for (int i = tid; i < a.nv; i += kStepThreads) {
+        if (a.grad_out) a.grad_out[i] = a.gt[i];
+        m = nanmax(m, fabs(a.gt[i]));
+      }
+      return block_max(m, sh);
+    }();
+    if (tid == 0) {
+      S.f = E;
+      S.gnorm = gm;
+    }
+    for (int i = tid; i < a.nv; i += kStepThreads) a.x[i] = a.xt[i];
+    __syncthreads();
+    finish(S, 1.0, h);
+    return;
+  }
+  enum { A_BEGIN, A_FAIL, A_EVAL, A_STOP_OK, A_STOP_FAIL, A_STOP_CAP };
+  int act;
+  if (S.phase == PH_INIT) {
+    double ss = 0.0, m = 0.0;
+    for (int i = tid; i < a.nv; i += kStepThreads) {
+      const double gi = a.gt[i];
+      a.g[i] = gi;
+      a.p[i] = -gi;
+      ss += gi * gi;
+      m = nanmax(m, fabs(gi));
+    }
+    const double nrm2 = sqrt(block_sum(ss, sh));
+    const double gm = block_max(m, sh);
+    if (tid == 0) {
+      S.f = E;
+      S.f_prev = E + nrm2 / 2.0;
+      S.gnorm = gm;
+    }
+    __syncthreads();  // every thread reads S.gnorm next
+    act = A_BEGIN;
+  } else {
+    double d = 0.0;
+    for (int i = tid; i < a.nv; i += kStepThreads) d += a.gt[i] * a.p[i];
+    const double dphi = block_sum(d, sh);
+    if (tid == 0) s_act = ls_step(S, E, dphi);
+    __syncthreads();
+    const int task = s_act;
+    __syncthreads();
+    if (task == T_FG) {
+      act = A_EVAL;
+    } else if (task == T_CONV) {
+      double num = 0.0;
+      for (int i = tid; i < a.nv; i += kStepThreads) num += (a.gt[i] - a.g[i]) * a.gt[i];
+      const double v = block_sum(num, sh) / S.delta;
+      const double beta = v > 0.0 ? v : 0.0;
+      double pg = 0.0, gg = 0.0, m = 0.0;
+      for (int i = tid; i < a.nv; i += kStepThreads) {
+        const double gi = a.gt[i];
+        const double pi = -gi + beta * a.p[i];
+        a.pn[i] = pi;
+        pg += pi * gi;
+        gg += gi * gi;
+        m = nanmax(m, fabs(gi));
+      }
+      const double spg = block_sum(pg, sh), sgg = block_sum(gg, sh), gn1 = block_max(m, sh);
+      if (gn1 <= a.gtol || spg <= -0.01 * sgg) {
+        for (int i = tid; i < a.nv; i += kStepThreads) {
+          a.x[i] = a.xt[i];
+          a.g[i] = a.gt[i];
+          a.p[i] = a.pn[i];
+        }
+        if (tid == 0) {
+          S.f_prev = S.f;
+          S.f = E;
+          S.gnorm = gn1;
+          S.k += 1;
+          S.restarted = 0;
+        }
+        act = A_BEGIN;
+      } else {
+        act = A_FAIL;
+      }
+    } else {
+      act = A_FAIL;
+    }
+    __syncthreads();
+  }
+  // at most: fail -> begin (restarted) -> fail -> stop
+  for (int guard = 0; guard < 4; ++guard) {
+    if (act == A_FAIL) {
+      int ne = 0;
+      for (int i = tid; i < a.nv; i += kStepThreads) ne |= (a.p[i] != -a.g[i]);
+      const int alleq = __syncthreads_or(ne) == 0;
+      if (S.restarted || alleq) {
+        act = A_STOP_FAIL;
+      } else {
+        for (int i = tid; i < a.nv; i += kStepThreads) a.p[i] = -a.g[i];
+        __syncthreads();
+        if (tid == 0) S.restarted = 1;
+        act = A_BEGIN;
+      }
+      __syncthreads();
+    }
+    if (act == A_BEGIN) {
+      if (!(S.gnorm > a.gtol) || S.k >= a.maxiter) {
+        act = A_STOP_OK;
+      } else {
+        double gg = 0.0, gp = 0.0;
+        for (int i = tid; i < a.nv; i += kStepThreads) {
+          gg += a.g[i] * a.g[i];
+          gp += a.g[i] * a.p[i];
+        }
+        const double delta = block_sum(gg, sh), d0 = block_sum(gp, sh);
+        if (tid == 0) {
+          S.delta = delta;
+          double alpha1 = 1.0;
+          if (d0 != 0.0) {
+            const double v = 1.01 * 2 * (S.f - S.f_prev) / d0;
+            alpha1 = v < 1.0 ? v : 1.0;  // min(1, v) with Python's argument order
+            if (alpha1 < 0.0) alpha1 = 1.0;
+          }
+          s_act = ls_start(S, alpha1, S.f, d0);
+        }
+        __syncthreads();
+        act = s_act == T_FG ? A_EVAL : A_FAIL;
+        __syncthreads();
+      }
+    }
+    if (act != A_FAIL && act != A_BEGIN) break;
+  }
+  if (act == A_EVAL && S.nev >= S.maxev) act = A_STOP_CAP;
+  if (act == A_EVAL) {
+    const double stp = S.stp;
+    for (int i = tid; i < a.nv; i += kStepThreads) a.xt[i] = a.x[i] + stp * a.p[i];
+    __syncthreads();
+    prep_point(a, a.xt);
+    if (tid == 0) S.phase = PH_LS;
+    return;
+  }
+  __syncthreads();
+  const double success = act == A_STOP_CAP ? -1.0 : (act == A_STOP_OK && S.gnorm <= a.gtol ? 1.0 : 0.0);
+  finish(S, success, h);
+}
+
+// the occupations at the result (one CTA), then C^J, C^K (grid)
+__global__ void __launch_bounds__(kStepThreads) occ_final_kernel(const OccState* __restrict__ st) {
+  const OccArgs& a = st->a;
+  if (!a.n_out && !a.cj_out) return;
+  prep_point(a, a.x);
+  if (a.n_out)
+    for (int i = threadIdx.x; i < a.P; i += kStepThreads) a.n_out[i] = a.n[i];
+}
+
+// CJCKD8 (pnof.py:350-422) at the result's occupations, diagonals included:
+// C^J = 2 n n^T, C^K = n n^T, plus on S x W, W x S, W x W the fi fi^T and
+// +-nd12 nd12^T - nd nd^T terms; inside each pair block C^J = 0 and
+// C^K = sqrt(n_s n_w) (strong-weak), -sqrt(n_w n_w') (weak-weak).  The
+// elementwise order of the numpy expressions, without contraction.
+__global__ void __launch_bounds__(256) occ_cjck_kernel(const OccState* __restrict__ st) {
+  const OccArgs& a = st->a;
+  if (!a.cj_out || !a.ck_out) return;
+  const int P = a.P, nb = a.no1 + a.ndoc, na = nb;
+  const long long total = (long long)P * P;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / P), j = (int)(t - (long long)i * P);
+    const double ni = a.n[i], nj = a.n[j];
+    double cj = __dmul_rn(2.0, __dmul_rn(ni, nj));
+    double ck = __dmul_rn(ni, nj);
+    const bool Si = i >= a.no1 && i < nb, Sj = j >= a.no1 && j < nb, Wi = i >= na, Wj = j >= na;
+    if ((Si && Wj) || (Wi && Sj) || (Wi && Wj)) ck = __dadd_rn(ck, __dmul_rn(a.fi[i], a.fi[j]));
+    if ((Si && Wj) || (Wi && Sj))
+      ck = __dadd_rn(ck, __dsub_rn(__dmul_rn(a.nd12[i], a.nd12[j]), __dmul_rn(a.nd[i], a.nd[j])));
+    if (Wi && Wj) ck = __dadd_rn(ck, __dsub_rn(-__dmul_rn(a.nd12[i], a.nd12[j]), __dmul_rn(a.nd[i], a.nd[j])));
+    const int pi = a.pair_of[i], pj = a.pair_of[j];
+    if (pi >= 0 && pi == pj) {
+      const bool si = i == a.no1 + pi, sj = j == a.no1 + pj;
+      if (!(si && sj)) {
+        cj = 0.0;
+        if (si || sj)
+          ck = sqrt(__dmul_rn(a.n[si ? i : j], a.n[si ? j : i]));
+        else
+          ck = -sqrt(__dmul_rn(ni, nj));
+      }
+    }
+    a.cj_out[t] = cj;
+    a.ck_out[t] = ck;
+  }
+}
+
+// ---- workspace and graphs
+template <class Cv>
+void occ_layout(Cv& c, int P, int ndoc, int ncwo, OccState** state, OccArgs& a) {
+  const int nv = ndoc * ncwo, nbc = (P + kBch - 1) / kBch;
+  *state = c.template take<OccState>(1);
+  a.x = c.template take<double>(nv);
+  a.g = c.template take<double>(nv);
+  a.p = c.template take<double>(nv);
+  a.pn = c.template take<double>(nv);
+  a.xt = c.template take<double>(nv);
+  a.gt = c.template take<double>(nv);
+  a.nw = c.template take<double>(nv);
+  a.n = c.template take<double>(P);
+  a.nd = c.template take<double>(P);
+  a.nd12 = c.template take<double>(P);
+  a.fi = c.template take<double>(P);
+  a.fid = c.template take<double>(P);
+  a.sq = c.template take<double>(P);
+  a.rsq = c.template take<double>(P);
+  a.e = c.template take<double>(P);
+  a.en = c.template take<double>(P);
+  a.ns = c.template take<double>(ndoc);
+  a.F = c.template take<double>(ndoc);
+  a.dF = c.template take<double>(ndoc);
+  a.part = c.template take<double>((size_t)5 * P * nbc);
+  a.row = c.template take<double>((size_t)5 * P);
+  a.pair_of = c.template take<int>(P);
+  a.cls = c.template take<int>(P);
+  a.nv = nv;
+  a.nbc = nbc;
+}
+
+struct OccGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t init = nullptr;
+};
+
+std::mutex g_mu;
+// (context id, workspace) -> graph; a context re-created after
+// cudaDeviceReset has a new id, so a stale graph is never reused
+std::map<std::pair<unsigned long long, const void*>, OccGraph> g_graphs;
+
+int build_graph(OccState* st, OccGraph& og) {
+  cudaGraph_t g = nullptr;
+  GB_TRY(gb::cuda_status(cudaGraphCreate(&g, 0), "occ graph create"));
+  auto fail = [&](cudaError_t e, const char* where) {
+    cudaGraphDestroy(g);
+    return gb::cuda_status(e, where);
+  };
+  OccArgs dummy{};
+  void* ip[] = {&st, &dummy};
+  cudaKernelNodeParams kp{};
+  kp.func = (void*)occ_init_kernel;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(kStepThreads);
+  kp.kernelParams = ip;
+  cudaGraphNode_t init = nullptr, wn = nullptr, n1 = nullptr, n2 = nullptr, n3 = nullptr, n4 = nullptr,
+                  n5 = nullptr;
+  cudaError_t e = cudaGraphAddKernelNode(&init, g, nullptr, 0, &kp);
+  if (e != cudaSuccess) return fail(e, "occ graph: init node");
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "occ graph: conditional handle");
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  e = cudaGraphAddNode(&wn, g, &init, nullptr, 1, &cp);
+  if (e != cudaSuccess) return fail(e, "occ graph: while node");
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  void* sp[] = {&st};
+  void* hp[] = {&st, &h};
+  cudaKernelNodeParams r{};
+  r.func = (void*)occ_rows_kernel;
+  r.gridDim = dim3(kRowCtas);
+  r.blockDim = dim3(32);
+  r.kernelParams = sp;
+  e = cudaGraphAddKernelNode(&n1, body, nullptr, 0, &r);
+  if (e != cudaSuccess) return fail(e, "occ graph: rows node");
+  cudaKernelNodeParams rd{};
+  rd.func = (void*)occ_reduce_kernel;
+  rd.gridDim = dim3(kRedCtas);
+  rd.blockDim = dim3(32);
+  rd.kernelParams = sp;
+  e = cudaGraphAddKernelNode(&n2, body, &n1, 1, &rd);
+  if (e != cudaSuccess) return fail(e, "occ graph: reduce node");
+  cudaKernelNodeParams sk{};
+  sk.func = (void*)occ_step_kernel;
+  sk.gridDim = dim3(1);
+  sk.blockDim = dim3(kStepThreads);
+  sk.kernelParams = hp;
+  e = cudaGraphAddKernelNode(&n3, body, &n2, 1, &sk);
+  if (e != cudaSuccess) return fail(e, "occ graph: step node");
+  cudaKernelNodeParams fk{};
+  fk.func = (void*)occ_final_kernel;
+  fk.gridDim = dim3(1);
+  fk.blockDim = dim3(kStepThreads);
+  fk.kernelParams = sp;
+  e = cudaGraphAddKernelNode(&n4, g, &wn, 1, &fk);
+  if (e != cudaSuccess) return fail(e, "occ graph: final node");
+  cudaKernelNodeParams ck{};
+  ck.func = (void*)occ_cjck_kernel;
+  ck.gridDim = dim3(kCjckCtas);
+  ck.blockDim = dim3(256);
+  ck.kernelParams = sp;
+  e = cudaGraphAddKernelNode(&n5, g, &n4, 1, &ck);
+  if (e != cudaSuccess) return fail(e, "occ graph: cjck node");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
+  if (e != cudaSuccess) return fail(e, "occ graph: instantiate");
+  og.graph = g;
+  og.exec = exec;
+  og.init = init;
+  return GB_OK;
+}
+
+int occ_run(const double* gamma0, const double* J, const double* K, const double* H, int nbf5, int no1, int ndoc,
+            int ncwo, double gtol, int maxiter, int mode, double* gamma_out, double* grad_out, double* result,
+            double* n_out, double* cj_out, double* ck_out, void* ws, size_t ws_bytes, void* stream,
+            const char* name) {
+  gb::clear_error();
+  GB_REQUIRE(gamma0 && J && K && H && result && ws, GB_ERR_INVALID_ARG, "%s: null pointer", name);
+  GB_REQUIRE(mode == MODE_EVAL || gamma_out, GB_ERR_INVALID_ARG, "%s: null gamma_out", name);
+  GB_REQUIRE((cj_out == nullptr) == (ck_out == nullptr), GB_ERR_INVALID_ARG, "%s: give both cj12 and ck12 or neither",
+             name);
+  GB_REQUIRE(no1 >= 0 && ndoc >= 1 && ncwo >= 1 && (long long)no1 + (long long)ndoc * (1 + ncwo) <= nbf5,
+             GB_ERR_BAD_SHAPE, "%s: need no1 + ndoc (1 + ncwo) <= nbf5 (%d, %d, %d, %d)", name, no1, ndoc, ncwo,
+             nbf5);
+  GB_REQUIRE(maxiter >= 0 && gtol >= 0.0, GB_ERR_INVALID_ARG, "%s: need maxiter >= 0 and gtol >= 0", name);
+  GB_REQUIRE(reinterpret_cast<uintptr_t>(ws) % 256 == 0, GB_ERR_INVALID_ARG, "%s: workspace not 256-byte aligned",
+             name);
+  gb::SizeCarve sc;
+  OccState* dummy;
+  OccArgs a{};
+  occ_layout(sc, nbf5, ndoc, ncwo, &dummy, a);
+  GB_REQUIRE(ws_bytes >= sc.used, GB_ERR_WORKSPACE, "%s: workspace of %zu bytes, need %zu", name, ws_bytes, sc.used);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GB_TRY(gb::cuda_status(cudaStreamIsCapturing(s, &cs), name));
+  GB_REQUIRE(cs == cudaStreamCaptureStatusNone, GB_ERR_UNSUPPORTED, "%s: not capturable (runs its own graph)", name);
+  gb::Carve c(ws, ws_bytes);
+  OccState* st = nullptr;
+  occ_layout(c, nbf5, ndoc, ncwo, &st, a);
+  a.J = J;
+  a.K = K;
+  a.H = H;
+  a.gamma0 = gamma0;
+  a.gamma_out = gamma_out ? gamma_out : a.x;
+  a.grad_out = grad_out;
+  a.res = result;
+  a.n_out = n_out;
+  a.cj_out = cj_out;
+  a.ck_out = ck_out;
+  a.P = nbf5;
+  a.no1 = no1;
+  a.ndoc = ndoc;
+  a.ncwo = ncwo;
+  a.maxiter = maxiter;
+  a.mode = mode;
+  a.gtol = gtol;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const auto key = std::make_pair(gb::current_context_id(), (const void*)ws);
+  auto it = g_graphs.find(key);
+  if (it == g_graphs.end()) {
+    OccGraph og;
+    GB_TRY(build_graph(st, og));
+    it = g_graphs.emplace(key, og).first;
+  }
+  void* ip[] = {&st, &a};
+  cudaKernelNodeParams kp{};
+  kp.func = (void*)occ_init_kernel;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(kStepThreads);
+  kp.kernelParams = ip;
+  GB_TRY(gb::cuda_status(cudaGraphExecKernelNodeSetParams(it->second.exec, it->second.init, &kp), name));
+  const int pi = gb::prof_begin(name, s);
+  const cudaError_t e = cudaGraphLaunch(it->second.exec, s);
+  gb::prof_end(pi, s);
+  return gb::cuda_status(e, name);
+}
+
+}  // namespace
+
+extern "C" size_t gb_occ_workspace_bytes(int nbf5, int ndoc, int ncwo) {
+  if (nbf5 < 1 || ndoc < 1 || ncwo < 1) return 0;
+  gb::SizeCarve sc;
+  OccState* st;
+  OccArgs a{};
+  occ_layout(sc, nbf5, ndoc, ncwo, &st, a);
+  return sc.used;
+}
+
+extern "C" int gb_occ_minimize_dev(const double* gamma0, const double* J_MO, const double* K_MO,
+                                   const double* H_core, int nbf5, int no1, int ndoc, int ncwo, double gtol,
+                                   int maxiter, double* gamma_out, double* result, double* n_out, double* cj12_out,
+                                   double* ck12_out, void* ws, size_t ws_bytes, void* stream) {
+  return occ_run(gamma0, J_MO, K_MO, H_core, nbf5, no1, ndoc, ncwo, gtol, maxiter, MODE_MIN, gamma_out, nullptr,
+                 result, n_out, cj12_out, ck12_out, ws, ws_bytes, stream, "gb_occ_minimize_dev");
+}
+
+extern "C" int gb_occ_energy_grad_dev(const double* gamma, const double* J_MO, const double* K_MO,
+                                      const double* H_core, int nbf5, int no1, int ndoc, int ncwo, double* result,
+                                      double* grad, void* ws, size_t ws_bytes, void* stream) {
+  return occ_run(gamma, J_MO, K_MO, H_core, nbf5, no1, ndoc, ncwo, 0.0, 0, MODE_EVAL, nullptr, grad, result,
+                 nullptr, nullptr, nullptr, ws, ws_bytes, stream, "gb_occ_energy_grad_dev");
+}
+
+extern "C" int gb_occ_release(const void* ws) {
+  gb::clear_error();
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto it = g_graphs.begin(); it != g_graphs.end();) {
+    if (it->first.second == ws) {
+      cudaGraphExecDestroy(it->second.exec);
+      cudaGraphDestroy(it->second.graph);
+      it = g_graphs.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  return GB_OK;
+}

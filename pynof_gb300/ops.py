@@ -360,6 +360,79 @@ def rotate_orbital(y: torch.Tensor, C: torch.Tensor, nbf5: int, out: torch.Tenso
     return out
 
 
+class OccMinimizer:
+    """occoptr's minimisation of the occupation energy over gamma on the
+    device (``gb_occ_minimize_dev``; ``pynof/minimization.py:77-97``): scipy's
+    CG (Polak-Ribiere+, More-Thuente line search, gtol 1e-5 on ||g||_inf) over
+    E(gamma) of calcocce / calcoccg at fixed device J_MO, K_MO, H_core, as one
+    CUDA graph per minimisation with no host synchronisation.  Owns its
+    workspace (the library caches the graph per workspace) and its outputs;
+    one minimisation at a time per object, on the current stream."""
+
+    def __init__(self, nbf5: int, no1: int, ndoc: int, ncwo: int, device=None):
+        self.dims = (int(nbf5), int(no1), int(ndoc), int(ncwo))
+        self.nv = ndoc * ncwo
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._wn = _lib.query("gb_occ_workspace_bytes", nbf5, ndoc, ncwo)
+        if self._wn == 0:
+            raise ValueError(f"no occupation problem for nbf5={nbf5}, ndoc={ndoc}, ncwo={ncwo}")
+        self._ws = torch.empty(self._wn + 256, dtype=torch.uint8, device=self.device)
+        self._wp = (self._ws.data_ptr() + 255) & ~255
+
+        def z(*shape):
+            return torch.zeros(shape, dtype=_F64, device=self.device)
+
+        self.result = z(5)  # E, iterations, evaluations, success, ||g||_inf
+        self.gamma = z(self.nv)
+        self.grad = z(self.nv)
+        self.n = z(nbf5)
+        self.cj12 = z(nbf5, nbf5)
+        self.ck12 = z(nbf5, nbf5)
+
+    def _check(self, gamma, J, K, H):
+        P = self.dims[0]
+        _require(gamma, (self.nv,), "gamma")
+        _require(J, (P, P), "J_MO")
+        _require(K, (P, P), "K_MO")
+        _require(H, (P,), "H_core")
+
+    def minimize(self, gamma0, J_MO, K_MO, H_core, gtol: float = 1e-5, maxiter: int | None = None,
+                 coefficients: bool = True):
+        """Launch the minimisation from gamma0; returns the device tensors
+        (gamma, result, n, cj12, ck12) it fills (n, cj12, ck12 at the result;
+        None with ``coefficients=False``)."""
+        self._check(gamma0, J_MO, K_MO, H_core)
+        maxiter = 200 * self.nv if maxiter is None else int(maxiter)
+        co = (self.n, self.cj12, self.ck12) if coefficients else (None, None, None)
+        _lib.call("gb_occ_minimize_dev", _ptr(gamma0), _ptr(J_MO), _ptr(K_MO), _ptr(H_core), *self.dims,
+                  float(gtol), maxiter, _ptr(self.gamma), _ptr(self.result), *(_ptr(t) for t in co), self._wp,
+                  self._wn, _stream(self.device))
+        return (self.gamma, self.result) + co
+
+    def energy_grad(self, gamma, J_MO, K_MO, H_core):
+        """One evaluation: (result, grad) device tensors, result[0] = E."""
+        self._check(gamma, J_MO, K_MO, H_core)
+        _lib.call("gb_occ_energy_grad_dev", _ptr(gamma), _ptr(J_MO), _ptr(K_MO), _ptr(H_core), *self.dims,
+                  _ptr(self.result), _ptr(self.grad), self._wp, self._wn, _stream(self.device))
+        return self.result, self.grad
+
+    def close(self) -> None:
+        """Drop the library's cached graph for this workspace (after the
+        stream's work on it has finished)."""
+        if self._ws is not None:
+            torch.cuda.current_stream(self.device).synchronize()
+            _lib.call("gb_occ_release", self._wp)
+            self._ws = None
+
+    def __del__(self):
+        try:
+            if self._ws is not None and torch.cuda.is_available():
+                torch.cuda.synchronize(self.device)
+                _lib.call("gb_occ_release", self._wp)
+        except Exception:
+            pass
+
+
 class StreamGraph:
     """Work issued by this thread on ``stream`` between ``begin`` and ``end``,
     captured (thread-local mode) into a CUDA graph and replayed by

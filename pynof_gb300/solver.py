@@ -5,9 +5,12 @@ Restates the orbital / occupation optimisation of ``pynof.compute_energy``
 over the softmax gammas), ``orbopt_adam`` (``minimization.py:200-253``,
 AMSgrad on orbital rotations), ``order_occupations_softmax``
 (``guess.py:77-106``) and the convergence test on the two gradient norms --
-with every four-index contraction (``computeJKH_MO``, ``computeLagrange2``)
-and the orbital rotation (``rotate_orbital``, FP64 expm) on the GPU and the
-occupation-space math in FP64 on the host (:mod:`pynof_gb300.nof`).
+with every four-index contraction (``computeJKH_MO``, ``computeLagrange2``),
+the orbital rotation (``rotate_orbital``, FP64 expm) and, by default, the
+occupation optimiser (scipy's CG over calcocce / calcoccg as one device graph,
+:class:`ops.OccMinimizer`) on the GPU; the AMSgrad bookkeeping and the
+remaining occupation-space math run in FP64 on the host
+(:mod:`pynof_gb300.nof`).
 
 A :class:`Backend` owns one molecule's resident device state (b, its sliced
 form for the tensor-core path, H) and a CUDA stream, so several solves can
@@ -38,9 +41,16 @@ class Backend:
     once per (precision, number of expm squarings)."""
 
     def __init__(self, st, b, H, precision: str = "mixed", nslices: int = 6, device=None, stream=None,
-                 use_graphs: bool = True):
+                 use_graphs: bool = True, occupations: str = "device"):
+        if occupations not in ("device", "host"):
+            raise ValueError(f"occupations must be 'device' or 'host', got {occupations!r}")
         self.st = st
         self.use_graphs = use_graphs
+        # "device": occoptr's CG runs on the device (ops.OccMinimizer) at the
+        # device J_MO, K_MO, H_core; "host": scipy's CG over the compiled host
+        # evaluation (scipy's own iterates)
+        self.occupations = occupations
+        self._occ = None
         self._norm = ops.AntisymNorm(st.nbf, st.nbf5)
         self._graphs: dict = {}
         self._buf: dict | None = None
@@ -96,6 +106,33 @@ class Backend:
     def jkh_mo(self, C):
         with torch.cuda.stream(self.stream):
             return self._sync_host(*self._jkh_mo_dev(ops.to_device(C, self.device)))
+
+    # ---- occupations on the device ----------------------------------------
+    def _occ_min(self):
+        if self._occ is None:
+            st = self.st
+            self._occ = ops.OccMinimizer(st.nbf5, st.no1, st.ndoc, st.ncwo, self.device)
+        return self._occ
+
+    def occ_minimize(self, gamma, C):
+        """occoptr's CG at orbitals C on the device: J_MO, K_MO, H_core stay
+        on the device; returns host (E, iterations, success, gamma, n, cj12,
+        ck12) from one synchronisation."""
+        with torch.cuda.stream(self.stream):
+            J, K, Hc = self._jkh_mo_dev(ops.to_device(C, self.device))
+            om = self._occ_min()
+            gam, res, n, cj, ck = om.minimize(ops.to_device(gamma, self.device), J, K, Hc)
+            gam, res, n, cj, ck = self._sync_host(gam, res, n, cj, ck)
+        if res[3] < 0:
+            raise RuntimeError("occupation minimiser reached its evaluation cap")
+        return float(res[0]), int(res[1]), bool(res[3] == 1.0), gam, n, cj, ck
+
+    def occ_gradient(self, gamma, C):
+        """dE/dgamma (calcoccg) at orbitals C, evaluated on the device."""
+        with torch.cuda.stream(self.stream):
+            J, K, Hc = self._jkh_mo_dev(ops.to_device(C, self.device))
+            _, grad = self._occ_min().energy_grad(ops.to_device(gamma, self.device), J, K, Hc)
+            return self._sync_host(grad)[0]
 
     # ---- device-resident orbital steps ---------------------------------
     def _static(self):
@@ -217,7 +254,11 @@ def calcorbg(y, n, cj12, ck12, C, be, p):
 
 
 def occoptr(gamma, C, be, p):
-    """``minimization.py:77-97``: CG over gamma at fixed orbitals."""
+    """``minimization.py:77-97``: CG over gamma at fixed orbitals -- on the
+    device when the backend's ``occupations`` is "device" (closed shell),
+    else scipy's CG over the compiled host evaluation."""
+    if p.ndoc > 0 and getattr(be, "occupations", "host") == "device" and nof.native_occ_ok(p):
+        return be.occ_minimize(gamma, C)
     J_MO, K_MO, H_core = be.jkh_mo(C)
     E, nit, success = 0.0, 0, True
     if p.ndoc > 0:
@@ -325,11 +366,14 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
         E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
         C, gamma = nof.order_occupations_softmax(C, gamma, p)
         g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
-        J_MO, K_MO, H_core = be.jkh_mo(C)
-        if nof.native_occ_ok(p):
-            g_occ = np.linalg.norm(nof.OccFunction(J_MO, K_MO, H_core, p)(gamma)[1])
+        if p.ndoc > 0 and getattr(be, "occupations", "host") == "device" and nof.native_occ_ok(p):
+            g_occ = np.linalg.norm(be.occ_gradient(gamma, C))
         else:
-            g_occ = np.linalg.norm(nof.calcoccg_fast(gamma, J_MO, K_MO, H_core, p))
+            J_MO, K_MO, H_core = be.jkh_mo(C)
+            if nof.native_occ_ok(p):
+                g_occ = np.linalg.norm(nof.OccFunction(J_MO, K_MO, H_core, p)(gamma)[1])
+            else:
+                g_occ = np.linalg.norm(nof.calcoccg_fast(gamma, J_MO, K_MO, H_core, p))
         for k, v in (("E_orb", E_orb), ("E_occ", E_occ), ("g_orb", g_orb), ("g_occ", g_occ), ("nit_orb", nit_orb),
                      ("nit_occ", nit_occ), ("precision", be.precision)):
             hist[k].append(v)
