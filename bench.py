@@ -57,11 +57,12 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--nslices", type=int, default=6)
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 comparison leg (0 = skip)")
-    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision", "mo", "hostlink"], default="jk",
+    ap.add_argument("--mode", choices=["jk", "batch", "serve", "precision", "mo", "hostlink", "occ"], default="jk",
                     help="jk: one nbf=600 build (the headline); batch: 64 molecules; serve: NOF solve stream; "
                          "precision: every split form against FP64 (J, K, E, orbital gradient); "
                          "mo: computeJKH_MO and computeLagrange2 per kernel, with the bandwidth kernels' GB/s; "
-                         "hostlink: device <-> pinned host copy rates at the size of one build's J, K")
+                         "hostlink: device <-> pinned host copy rates at the size of one build's J, K; "
+                         "occ: occoptr's CG on the device against scipy's on the host")
     ap.add_argument("--nmol", type=int, default=64)
     ap.add_argument("--batch-nbf-max", type=int, default=400, help="largest nbf of the batch (batch mode)")
     ap.add_argument("--requests", type=int, default=16)
@@ -72,6 +73,7 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--maxit", type=int, default=200)
     ap.add_argument("--time-limit", type=float, default=None, help="seconds per served solve (serve mode)")
+    ap.add_argument("--occ-nbf", default="60,300,600", help="nbf of the occupation problems (occ mode)")
     return ap.parse_args()
 
 
@@ -818,6 +820,73 @@ def run_hostlink(args):
     print(json.dumps(line), flush=True)
 
 
+def run_occ(args):
+    """occoptr's minimisation over gamma (scipy's CG on calcocce / calcoccg,
+    minimization.py:77-97) at the sizes of ``--occ-nbf`` (ndoc = nbf // 10,
+    ncwo = 4, nbf5 = nbf / 2; 300 and 600 are the c2 and c3 shapes): on the
+    device (ops.OccMinimizer,
+    one CUDA graph per minimisation) and as the host form (scipy's CG over
+    the compiled host evaluation).  J_MO, K_MO, H_core come from the FP64
+    device computeJKH_MO at seeded synthetic orbitals; gamma starts from the
+    reference's softmax guess.  Device: CUDA events over --steps
+    minimisations after --warmup (``e2e_ms`` adds the copy of gamma, n,
+    C^J, C^K to the host and the synchronisation, as the solver makes it);
+    host: wall clock, best of 3."""
+    import scipy.optimize
+    import torch
+
+    from pynof_gb300 import nof, ops, synthetic
+
+    torch.cuda.set_device(0)
+    sizes = {}
+    for nbf in (int(x) for x in args.occ_nbf.split(",")):
+        name, st = f"nbf={nbf}", synthetic.Structure.for_nbf(nbf)
+        b, C, H, _ = synthetic.make_inputs(st, seed=0)
+        db = ops.to_device(b)
+        del b
+        J, K, Hc = ops.jkh_mo_ri(ops.to_device(C), ops.to_device(H), db, st.nbf5)
+        del db
+        g0 = nof.gamma_guess_softmax(st)
+        dg = ops.to_device(g0)
+        om = ops.OccMinimizer(st.nbf5, st.no1, st.ndoc, st.ncwo)
+        for _ in range(args.warmup):
+            om.minimize(dg, J, K, Hc)
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            om.minimize(dg, J, K, Hc)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res = om.result.cpu().numpy()
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            outs = om.minimize(dg, J, K, Hc)
+            [o.cpu() for o in (outs[0], outs[1], outs[2], outs[3], outs[4])]
+            t.append(time.perf_counter() - t0)
+        fn = nof.OccFunction(J.cpu().numpy(), K.cpu().numpy(), Hc.cpu().numpy(), st)
+        th = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ref = scipy.optimize.minimize(fn, g0, jac=True, method="CG")
+            th.append(time.perf_counter() - t0)
+        sizes[name] = {"nbf5": st.nbf5, "nv": st.nv,
+                       "device": {"ms": ms, "iterations": int(res[1]), "evaluations": int(res[2]),
+                                  "us_per_evaluation": 1e3 * ms / res[2], "e2e_ms": 1e3 * min(t),
+                                  "E": float(res[0]), "success": bool(res[3] == 1.0)},
+                       "host_scipy": {"ms": 1e3 * min(th), "iterations": int(ref.nit), "evaluations": int(ref.nfev),
+                                      "E": float(ref.fun)},
+                       "speedup_e2e": min(th) / min(t), "E_rel_diff": abs(res[0] - ref.fun) / abs(ref.fun)}
+        om.close()
+    line = {"mode": "occ", "metric": "occupation minimisation time (occoptr, scipy's CG on calcocce/calcoccg)",
+            "unit": "ms", "data": "synthetic (J_MO, K_MO, H_core from the FP64 device computeJKH_MO)",
+            "config": {"steps": args.steps, "warmup": args.warmup, "gtol": 1e-5}, "sizes": sizes}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -832,6 +901,8 @@ def main():
         run_mo(args)
     elif args.mode == "hostlink":
         run_hostlink(args)
+    elif args.mode == "occ":
+        run_occ(args)
     else:
         run_ours(args)
 

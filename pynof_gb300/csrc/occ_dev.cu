@@ -13,12 +13,21 @@
 //    and the gradient of calcoccg, pnof.py:1004-1033 with der_CJCKD8,
 //    pnof.py:425-525): occ_rows_kernel, one warp per (32 orbitals a, 16
 //    orbitals b) item on a fixed grid, lanes over a so that J[b][a] and
-//    K[b][a] are read coalesced; per a: the energy terms in a compensated
-//    (Neumaier) sum, the dE/dn term and the two sums that give dE/dnd;
-//  - occ_reduce_kernel: one warp per a over its b chunks (fixed tree order);
+//    K[b][a] are read coalesced; per a: the energy terms, the dE/dn term and
+//    the two sums that give dE/dnd, each summed over the item's 16 pairs in
+//    a pairwise tree; the last warp to finish an a-group (an atomic count per
+//    group, no waiting) adds the group's items;
 //  - occ_step_kernel (one CTA): the diagonal and same-pair terms, the chain
-//    rule through nd = n F(n_s), g = dn^T e, and the energy -- the same
-//    assembly as the host loop of occ_host.cu.
+//    rule through nd = n F(n_s), g = dn^T e, and the energy -- the assembly
+//    of the host loop of occ_host.cu, summed in pairwise trees.
+//
+// GB300's FP64 unit has a long dependent latency (~64 clocks for an add or
+// FMA, several hundred for a division or square root, ~1000 for exp), so the
+// kernels are laid out for short FP64 dependency chains: every exponential
+// of a trial point in its own thread, the pair loop unrolled with masks,
+// tree sums, and the conjugate-gradient scalars of one evaluation from one
+// fused block reduction (the next search's g.g and g.p follow from it
+// algebraically).
 //
 // The minimiser is scipy's CG as scipy 1.18 runs it: Polak-Ribiere+ with the
 // sufficient-descent check, the first trial step from the previous decrease,
@@ -30,10 +39,11 @@
 // steepest descent once and otherwise stops at the current point.
 //
 // One CUDA graph per workspace runs a whole minimisation: an init kernel, a
-// WHILE conditional node whose body is rows -> reduce -> step (the step kernel
-// clears the condition when the minimiser stops), then the occupations and
-// C^J, C^K at the result.  The number of evaluations is capped at
-// 1 + 200 (maxiter + 1): a minimiser that reaches the cap reports success -1.
+// WHILE conditional node whose body is four rounds of rows -> step (the step
+// kernel clears the condition when the minimiser stops and the kernels after
+// it return at once), then the occupations and C^J, C^K at the result.  The
+// number of evaluations is capped at 1 + 200 (maxiter + 1): a minimiser that
+// reaches the cap reports success -1.
 //
 // All arithmetic is FP64 (GB300's FP64 rate is low, so the O(nbf5^2) pair
 // work is spread over the whole GPU and the single-CTA work is O(nbf5)).
@@ -49,7 +59,7 @@ namespace {
 
 constexpr int kStepThreads = 256;
 constexpr int kRowCtas = 4 * 152;  // rows kernel: one warp per CTA, grid-stride over items
-constexpr int kRedCtas = 2 * 152;  // reduce kernel: one warp per CTA
+constexpr int kUnroll = 4;         // evaluations per round of the WHILE node
 constexpr int kCjckCtas = 2 * 152;
 constexpr int kBch = 16;           // orbitals b per item of the rows kernel
 constexpr double kHCut = 0.02 * 1.4142135623730951;
@@ -71,17 +81,18 @@ struct OccArgs {
   double *e, *en;                               // P
   double *ns, *F, *dF;                          // ndoc
   double *nw;                                   // nv
-  double *part;                                 // 5 P nbc
-  double *row;                                  // 5 P
+  double *part;                                 // 4 P nbc (per item: energy, e, S1, S2)
+  double *row;                                  // 4 P (per orbital, all items)
   int *pair_of, *cls;                           // P
+  unsigned int* grp;                            // per a-group: items done
   int P, no1, ndoc, ncwo, nv, nbc, maxiter, mode;
   double gtol;
 };
 
 struct OccState {
   OccArgs a;
-  // conjugate gradients
-  double f, f_prev, gnorm, delta;
+  // conjugate gradients (delta = g.g, d0 = g.p of the next line search)
+  double f, f_prev, gnorm, delta, d0;
   int k, nev, maxev, phase, restarted;
   // More-Thuente line search
   double stp, finit, ginit, gtest, width, width1, stx, fx, gx, sty, fy, gy, stmin, stmax;
@@ -93,109 +104,87 @@ __device__ __forceinline__ int weak_of(const OccArgs& a, int p, int j) {
 }
 __device__ __forceinline__ int gam_of(const OccArgs& a, int p, int j) { return (a.ndoc - p - 1) + a.ndoc * j; }
 
-// Neumaier's compensated addition (A. Neumaier, ZAMM 54 (1974) 39-51).
-__device__ __forceinline__ void comp_add(double& s, double& c, double x) {
-  const double t = s + x;
-  c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
-  s = t;
-}
-
-// NaN-propagating maximum of |v| (numpy's max of abs)
+// NaN-propagating maximum (numpy's max)
 __device__ __forceinline__ double nanmax(double a, double b) { return (a > b || a != a) ? a : b; }
 
-// ---- deterministic block reductions (fixed tree; every thread gets the value)
-__device__ double block_sum(double v, double* sh) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = l < kStepThreads / 32 ? sh[l] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (l == 0) sh[32] = v;
-  }
-  __syncthreads();
-  return sh[32];
-}
-
-__device__ double block_max(double v, double* sh) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = l < kStepThreads / 32 ? sh[l] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    if (l == 0) sh[32] = v;
-  }
-  __syncthreads();
-  return sh[32];
-}
-
-__device__ double block_comp(double s, double c, double* sh) {
+// ---- deterministic block reductions (fixed tree; every thread gets the
+// values): NS sums and, with MAX, a NaN-propagating maximum in slot NS
+template <int NS, bool MAX>
+__device__ void block_reduce(double (&v)[NS + (MAX ? 1 : 0)], double* sh) {
+  constexpr int NV = NS + (MAX ? 1 : 0);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   for (int o = 16; o > 0; o >>= 1) {
-    const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
-    if (l + o < 32) {
-      comp_add(s, c, s2);
-      comp_add(s, c, c2);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const double y = __shfl_down_sync(0xffffffffu, v[q], o);
+      v[q] = (MAX && q == NS) ? nanmax(v[q], y) : v[q] + y;
     }
   }
   __syncthreads();
-  if (l == 0) {
-    sh[w] = s;
-    sh[8 + w] = c;
-  }
+  if (l == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q * 8 + w] = v[q];
   __syncthreads();
   if (w == 0) {
-    s = l < kStepThreads / 32 ? sh[l] : 0.0;
-    c = l < kStepThreads / 32 ? sh[8 + l] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) {
-      const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
-      if (l + o < 32) {
-        comp_add(s, c, s2);
-        comp_add(s, c, c2);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = l < kStepThreads / 32 ? sh[q * 8 + l] : 0.0;
+    for (int o = 4; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        const double y = __shfl_down_sync(0xffffffffu, v[q], o);
+        v[q] = (MAX && q == NS) ? nanmax(v[q], y) : v[q] + y;
       }
     }
-    if (l == 0) sh[32] = s + c;
+    if (l == 0)
+#pragma unroll
+      for (int q = 0; q < NV; ++q) sh[64 + q] = v[q];
   }
   __syncthreads();
-  return sh[32];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = sh[64 + q];
+  __syncthreads();
 }
 
 // ---- the trial point's per-orbital quantities (all threads of one CTA)
 __device__ void prep_point(const OccArgs& a, const double* __restrict__ x) {
-  const int tid = threadIdx.x;
-  for (int p = tid; p < a.ndoc; p += kStepThreads) {
-    double top = -INFINITY, den = 1.0;
-    for (int j = 0; j < a.ncwo; ++j) top = fmax(top, x[gam_of(a, p, j)]);
+  const int tid = threadIdx.x, nd = a.ndoc, nc = a.ncwo;
+  // one exponential per logit, all at once (a pair with a logit past exp's
+  // range is redone with its largest logit below)
+  for (int t = tid; t < a.nv; t += kStepThreads) {
+    const int j = t / nd, p = nd - 1 - (t - j * nd);  // t = gam_of(p, j)
+    a.nw[p * nc + j] = exp(fmin(x[t], 700.0));
+  }
+  __syncthreads();
+  for (int p = tid; p < nd; p += kStepThreads) {
+    double top = -INFINITY;
+    for (int j = 0; j < nc; ++j) top = fmax(top, x[gam_of(a, p, j)]);
+    double* w = a.nw + p * nc;
     double ns;
     if (top >= 700.0) {
       // logits past exp's range: the same softmax shifted by the largest one
-      den = exp(-top);
-      for (int j = 0; j < a.ncwo; ++j) den += exp(x[gam_of(a, p, j)] - top);
+      double den = exp(-top);
+      for (int j = 0; j < nc; ++j) den += exp(x[gam_of(a, p, j)] - top);
       ns = exp(-top) / den;
-      for (int j = 0; j < a.ncwo; ++j) a.nw[p * a.ncwo + j] = exp(x[gam_of(a, p, j)] - top) / den;
+      for (int j = 0; j < nc; ++j) w[j] = exp(x[gam_of(a, p, j)] - top) / den;
     } else {
-      for (int j = 0; j < a.ncwo; ++j) den += exp(fmin(x[gam_of(a, p, j)], 700.0));
+      double den = 1.0;
+      for (int j = 0; j < nc; ++j) den += w[j];
       ns = 1.0 / den;
-      for (int j = 0; j < a.ncwo; ++j) a.nw[p * a.ncwo + j] = exp(fmin(x[gam_of(a, p, j)], 700.0)) / den;
+      for (int j = 0; j < nc; ++j) w[j] = w[j] / den;
     }
     a.ns[p] = ns;
     a.n[p] = ns;
-    for (int j = 0; j < a.ncwo; ++j) a.n[weak_of(a, p, j)] = a.nw[p * a.ncwo + j];
+    for (int j = 0; j < nc; ++j) a.n[weak_of(a, p, j)] = w[j];
   }
   __syncthreads();
-  for (int p = tid; p < a.ndoc; p += kStepThreads) {
+  for (int p = tid; p < nd; p += kStepThreads) {
     const int s = a.no1 + p;
     const double coc = (1.0 - a.n[s]) / kHCut;
     const double F = exp(-coc * coc);
     a.F[p] = F;
     a.dF[p] = 2.0 * coc / kHCut;  // (1/F) dF/dn_s
     a.nd[s] = a.n[s] * F;
-    for (int j = 0; j < a.ncwo; ++j) {
+    for (int j = 0; j < nc; ++j) {
       const int w = weak_of(a, p, j);
       a.nd[w] = a.n[w] * F;
     }
@@ -204,128 +193,131 @@ __device__ void prep_point(const OccArgs& a, const double* __restrict__ x) {
   for (int i = tid; i < a.P; i += kStepThreads) {
     const double ni = a.n[i];
     const double fi = sqrt(fmax(ni * (1.0 - ni), 0.0));
+    const double sq = sqrt(ni);
     a.nd12[i] = sqrt(a.nd[i]);
     a.fi[i] = fi;
     a.fid[i] = i < a.no1 ? 0.0 : (1.0 - 2.0 * ni) / (2.0 * fmax(fi, 1e-15));
-    a.sq[i] = sqrt(ni);
-    a.rsq[i] = 1.0 / sqrt(fmax(ni, 1e-15));
+    a.sq[i] = sq;
+    a.rsq[i] = ni >= 1e-15 ? 1.0 / sq : 1.0 / sqrt(1e-15);
   }
   __syncthreads();
 }
 
-// ---- pair sums over b for 32 orbitals a
+// Pairwise sum of kBch values.
+__device__ __forceinline__ double tree16(double (&t)[kBch]) {
+#pragma unroll
+  for (int h = kBch / 2; h > 0; h >>= 1)
+#pragma unroll
+    for (int u = 0; u < h; ++u) t[u] += t[u + h];
+  return t[0];
+}
+
+// ---- pair sums over b for 32 orbitals a, then (last warp of the a-group)
+// the group's items added per orbital
 __global__ void __launch_bounds__(32) occ_rows_kernel(const OccState* __restrict__ st) {
   const OccArgs& a = st->a;
   if (st->phase == PH_DONE) return;
   const int P = a.P, nbc = a.nbc, lane = threadIdx.x;
   const int nag = (P + 31) / 32;
+  const size_t plane = (size_t)P * nbc;
   for (int it = blockIdx.x; it < nag * nbc; it += gridDim.x) {
     const int ag = it / nbc, bc = it - ag * nbc;
     const int i = ag * 32 + lane;
-    if (i >= P) continue;
-    const int pa = a.pair_of[i], ca = a.cls[i];
-    const double ni = a.n[i], fii = a.fi[i], fidi = a.fid[i], nd12i = a.nd12[i], ndi = a.nd[i];
-    double Es = 0.0, Ec = 0.0, ea = 0.0, S1 = 0.0, S2 = 0.0;
-    const int b0 = bc * kBch, b1 = min(P, b0 + kBch);
-    for (int b = b0; b < b1; ++b) {
-      if (b == i || (pa >= 0 && a.pair_of[b] == pa)) continue;
-      const double Jba = a.J[(size_t)b * P + i], Kba = a.K[(size_t)b * P + i];
-      const double nb = a.n[b];
+    const bool live = i < P;
+    const int ii = live ? i : P - 1;
+    const int pa = a.pair_of[ii], ca = a.cls[ii];
+    const double ni = a.n[ii], fii = a.fi[ii], fidi = a.fid[ii], nd12i = a.nd12[ii], ndi = a.nd[ii];
+    double tE[kBch], tea[kBch], tS1[kBch], tS2[kBch];
+    const int b0 = bc * kBch;
+#pragma unroll
+    for (int u = 0; u < kBch; ++u) {
+      const int b = min(b0 + u, P - 1);
+      const bool ok = b0 + u < P && b != ii && !(pa >= 0 && a.pair_of[b] == pa);
+      const double Jba = a.J[(size_t)b * P + ii], Kba = a.K[(size_t)b * P + ii];
+      const double nb = a.n[b], fib = a.fi[b], nd12b = a.nd12[b], ndb = a.nd[b];
       const int cb = a.cls[b];
-      ea += 4.0 * nb * Jba;
-      double ck = ni * nb, dck = nb;
+      double ck = ni * nb, dck = nb, s1 = 0.0, s2 = 0.0;
       if ((ca == 1 && cb == 2) || (ca == 2 && cb >= 1)) {
         const double sg = (ca == 2 && cb == 2) ? -1.0 : 1.0;
-        ck += fii * a.fi[b] + sg * nd12i * a.nd12[b] - ndi * a.nd[b];
-        dck += fidi * a.fi[b];
-        S1 += sg * a.nd12[b] * Kba;
-        S2 += a.nd[b] * Kba;
+        ck += fii * fib + sg * nd12i * nd12b - ndi * ndb;
+        dck += fidi * fib;
+        s1 = sg * nd12b * Kba;
+        s2 = ndb * Kba;
       }
-      comp_add(Es, Ec, 2.0 * ni * nb * Jba - ck * Kba);
-      ea -= 2.0 * dck * Kba;
+      tE[u] = ok ? 2.0 * ni * nb * Jba - ck * Kba : 0.0;
+      tea[u] = ok ? 4.0 * nb * Jba - 2.0 * dck * Kba : 0.0;
+      tS1[u] = ok ? s1 : 0.0;
+      tS2[u] = ok ? s2 : 0.0;
     }
-    double* q = a.part + (size_t)i * nbc + bc;
-    const size_t plane = (size_t)P * nbc;
-    q[0] = Es;
-    q[plane] = Ec;
-    q[2 * plane] = ea;
-    q[3 * plane] = S1;
-    q[4 * plane] = S2;
-  }
-}
-
-// ---- per orbital a: its b chunks in a fixed tree order
-__global__ void __launch_bounds__(32) occ_reduce_kernel(const OccState* __restrict__ st) {
-  const OccArgs& a = st->a;
-  if (st->phase == PH_DONE) return;
-  const int P = a.P, nbc = a.nbc, l = threadIdx.x;
-  const size_t plane = (size_t)P * nbc;
-  for (int i = blockIdx.x; i < P; i += gridDim.x) {
-    const double* q = a.part + (size_t)i * nbc;
-    double s = 0.0, c = 0.0, ea = 0.0, S1 = 0.0, S2 = 0.0;
-    for (int bc = l; bc < nbc; bc += 32) {
-      comp_add(s, c, q[bc]);
-      comp_add(s, c, q[plane + bc]);
-      ea += q[2 * plane + bc];
-      S1 += q[3 * plane + bc];
-      S2 += q[4 * plane + bc];
+    const double vE = tree16(tE), vea = tree16(tea), vS1 = tree16(tS1), vS2 = tree16(tS2);
+    double* q = a.part + (size_t)ii * nbc + bc;
+    if (live) {
+      q[0] = vE;
+      q[plane] = vea;
+      q[2 * plane] = vS1;
+      q[3 * plane] = vS2;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
-      const double e2 = __shfl_down_sync(0xffffffffu, ea, o), x2 = __shfl_down_sync(0xffffffffu, S1, o),
-                   y2 = __shfl_down_sync(0xffffffffu, S2, o);
-      if (l + o < 32) {
-        comp_add(s, c, s2);
-        comp_add(s, c, c2);
-        ea += e2;
-        S1 += x2;
-        S2 += y2;
+    // the last of the group's nbc items adds them up (the counter is left at
+    // zero for the next evaluation)
+    __threadfence();
+    __syncwarp();  // every lane's partials are visible before the count moves
+    unsigned int done = 0;
+    if (lane == 0) done = atomicAdd(a.grp + ag, 1u);
+    done = __shfl_sync(0xffffffffu, done, 0);
+    if (done == (unsigned int)nbc - 1) {
+      __threadfence();
+      if (live) {
+        const double* r = a.part + (size_t)i * nbc;
+        double sE = 0.0, sea = 0.0, sS1 = 0.0, sS2 = 0.0;
+        for (int c = 0; c < nbc; ++c) {
+          sE += __ldcg(r + c);
+          sea += __ldcg(r + plane + c);
+          sS1 += __ldcg(r + 2 * plane + c);
+          sS2 += __ldcg(r + 3 * plane + c);
+        }
+        a.row[i] = sE;
+        a.row[P + i] = sea;
+        a.row[2 * P + i] = sS1;
+        a.row[3 * P + i] = sS2;
       }
-    }
-    if (l == 0) {
-      a.row[i] = s;
-      a.row[P + i] = c;
-      a.row[2 * P + i] = ea;
-      a.row[3 * P + i] = S1;
-      a.row[4 * P + i] = S2;
+      if (lane == 0) a.grp[ag] = 0;
     }
   }
 }
 
-// ---- energy and gradient at the trial point from the reduced rows (one CTA)
+// ---- energy and gradient at the trial point from the orbitals' sums (one CTA)
 __device__ double assemble(const OccArgs& a, double* sh) {
   const int P = a.P, tid = threadIdx.x;
-  double es = 0.0, ec = 0.0;
+  double es = 0.0;
   for (int i = tid; i < P; i += kStepThreads) {
     const double d = 2.0 * a.H[i] + a.J[(size_t)i * P + i];
-    comp_add(es, ec, a.n[i] * d);
-    comp_add(es, ec, a.row[i]);
-    comp_add(es, ec, a.row[P + i]);
-    a.e[i] = d + a.row[2 * P + i];
-    a.en[i] = -2.0 * (a.row[3 * P + i] / (2.0 * fmax(a.nd12[i], 1e-15)) - a.row[4 * P + i]);
+    es += a.n[i] * d + a.row[i];
+    a.e[i] = d + a.row[P + i];
+    a.en[i] = -2.0 * (a.row[2 * P + i] / (2.0 * fmax(a.nd12[i], 1e-15)) - a.row[3 * P + i]);
   }
   __syncthreads();
   // pairs inside one pair block: C^J = 0; C^K = sqrt(n_s n_w) (strong-weak),
   // -sqrt(n_w n_w') (weak-weak)
   for (int p = tid; p < a.ndoc; p += kStepThreads) {
     const int s = a.no1 + p;
-    double e_s = a.e[s];
+    double e_s = a.e[s], ep = 0.0;
     for (int j = 0; j < a.ncwo; ++j) {
       const int w = weak_of(a, p, j);
       const double Kws = a.K[(size_t)w * P + s], Ksw = a.K[(size_t)s * P + w];
-      comp_add(es, ec, -(a.sq[s] * a.sq[w]) * (Kws + Ksw));
+      double ew = 0.0, ej = -(a.sq[s] * a.sq[w]) * (Kws + Ksw);
       e_s -= a.sq[w] * a.rsq[s] * Kws;
-      double e_w = a.e[w] - a.sq[s] * a.rsq[w] * Ksw;
       for (int j2 = 0; j2 < a.ncwo; ++j2) {
         if (j2 == j) continue;
         const int w2 = weak_of(a, p, j2);
         const double Kw2w = a.K[(size_t)w2 * P + w];
-        comp_add(es, ec, a.sq[w] * a.sq[w2] * Kw2w);
-        e_w += a.sq[w2] * a.rsq[w] * Kw2w;
+        ej += a.sq[w] * a.sq[w2] * Kw2w;
+        ew += a.sq[w2] * Kw2w;
       }
-      a.e[w] = e_w;
+      ep += ej;
+      a.e[w] = a.e[w] - a.sq[s] * a.rsq[w] * Ksw + a.rsq[w] * ew;
     }
     a.e[s] = e_s;
+    es += ep;
   }
   __syncthreads();
   // nd_s = n_s F(n_s), nd_w = n_w F(n_s): chain dE/dnd to the occupations
@@ -350,7 +342,9 @@ __device__ double assemble(const OccArgs& a, double* sh) {
       a.gt[gam_of(a, p, j)] = -a.ns[p] * w * a.e[p] + w * a.e[weak_of(a, p, j)] - w * wsum;
     }
   }
-  return block_comp(es, ec, sh);  // synchronises
+  double v[1] = {es};
+  block_reduce<1, false>(v, sh);  // synchronises
+  return v[0];
 }
 
 // ---- More & Thuente, one safeguarded step (section 4 of the paper)
@@ -530,6 +524,7 @@ __global__ void __launch_bounds__(kStepThreads) occ_init_kernel(OccState* st, Oc
     a.cls[i] = i < a.no1 ? 0 : (i < nb ? 1 : 2);  // 1: strong set S, 2: weak set W
   }
   __syncthreads();
+  for (int g = tid; g < (a.P + 31) / 32; g += kStepThreads) a.grp[g] = 0u;
   for (int p = tid; p < a.ndoc; p += kStepThreads) {
     a.pair_of[a.no1 + p] = p;
     for (int j = 0; j < a.ncwo; ++j) a.pair_of[weak_of(a, p, j)] = p;
@@ -556,32 +551,50 @@ __device__ void finish(OccState& S, double success, cudaGraphConditionalHandle h
   }
 }
 
+// The state word by word between global and shared memory.
+__device__ __forceinline__ void copy_state(OccState* dst, const OccState* src) {
+  static_assert(sizeof(OccState) % 8 == 0, "OccState in 8-byte words");
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(OccState) / 8); i += blockDim.x) d[i] = s[i];
+}
+
+__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h);
+
 __global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h) {
-  __shared__ double sh[40];
+  __shared__ double sh[72];
   __shared__ int s_act;
-  OccState& S = *st;
-  const OccArgs& a = S.a;
-  const int tid = threadIdx.x;
-  if (S.phase == PH_DONE) {
-    if (tid == 0) cudaGraphSetConditional(h, 0);
+  // the step works on a copy in shared memory: its scalars and the array
+  // pointers are read there, not from global memory behind every store
+  __shared__ OccState S;
+  if (st->phase == PH_DONE) {
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, 0);
     return;
   }
+  copy_state(&S, st);
+  __syncthreads();
+  step_body(S, sh, s_act, h);
+  __syncthreads();
+  copy_state(st, &S);
+}
+
+__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h) {
+  const OccArgs& a = S.a;
+  const int tid = threadIdx.x;
   const double E = assemble(a, sh);
   if (tid == 0) S.nev += 1;
   if (a.mode == MODE_EVAL) {
-    const double gm = [&] {
-      double m = 0.0;
-      for (int i = tid; i < a.nv; i += kStepThreads) {
-        if (a.grad_out) a.grad_out[i] = a.gt[i];
-        m = nanmax(m, fabs(a.gt[i]));
-      }
-      return block_max(m, sh);
-    }();
+    double v[1] = {0.0};
+    for (int i = tid; i < a.nv; i += kStepThreads) {
+      if (a.grad_out) a.grad_out[i] = a.gt[i];
+      a.x[i] = a.xt[i];
+      v[0] = nanmax(v[0], fabs(a.gt[i]));
+    }
+    block_reduce<0, true>(v, sh);
     if (tid == 0) {
       S.f = E;
-      S.gnorm = gm;
+      S.gnorm = v[0];
     }
-    for (int i = tid; i < a.nv; i += kStepThreads) a.x[i] = a.xt[i];
     __syncthreads();
     finish(S, 1.0, h);
     return;
@@ -589,58 +602,59 @@ __global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cu
   enum { A_BEGIN, A_FAIL, A_EVAL, A_STOP_OK, A_STOP_FAIL, A_STOP_CAP };
   int act;
   if (S.phase == PH_INIT) {
-    double ss = 0.0, m = 0.0;
+    double v[2] = {0.0, 0.0};  // g.g, max |g|
     for (int i = tid; i < a.nv; i += kStepThreads) {
       const double gi = a.gt[i];
       a.g[i] = gi;
       a.p[i] = -gi;
-      ss += gi * gi;
-      m = nanmax(m, fabs(gi));
+      v[0] += gi * gi;
+      v[1] = nanmax(v[1], fabs(gi));
     }
-    const double nrm2 = sqrt(block_sum(ss, sh));
-    const double gm = block_max(m, sh);
+    block_reduce<1, true>(v, sh);
     if (tid == 0) {
       S.f = E;
-      S.f_prev = E + nrm2 / 2.0;
-      S.gnorm = gm;
+      S.f_prev = E + sqrt(v[0]) / 2.0;
+      S.gnorm = v[1];
+      S.delta = v[0];
+      S.d0 = -v[0];
     }
     __syncthreads();  // every thread reads S.gnorm next
     act = A_BEGIN;
   } else {
-    double d = 0.0;
-    for (int i = tid; i < a.nv; i += kStepThreads) d += a.gt[i] * a.p[i];
-    const double dphi = block_sum(d, sh);
-    if (tid == 0) s_act = ls_step(S, E, dphi);
+    // one pass for the whole step: g1.p (the search's slope), (g1 - g).g1,
+    // g1.g1, max |g1| at the trial point
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = tid; i < a.nv; i += kStepThreads) {
+      const double gi = a.gt[i];
+      v[0] += gi * a.p[i];
+      v[1] += (gi - a.g[i]) * gi;
+      v[2] += gi * gi;
+      v[3] = nanmax(v[3], fabs(gi));
+    }
+    block_reduce<3, true>(v, sh);
+    if (tid == 0) s_act = ls_step(S, E, v[0]);
     __syncthreads();
     const int task = s_act;
     __syncthreads();
     if (task == T_FG) {
       act = A_EVAL;
     } else if (task == T_CONV) {
-      double num = 0.0;
-      for (int i = tid; i < a.nv; i += kStepThreads) num += (a.gt[i] - a.g[i]) * a.gt[i];
-      const double v = block_sum(num, sh) / S.delta;
-      const double beta = v > 0.0 ? v : 0.0;
-      double pg = 0.0, gg = 0.0, m = 0.0;
-      for (int i = tid; i < a.nv; i += kStepThreads) {
-        const double gi = a.gt[i];
-        const double pi = -gi + beta * a.p[i];
-        a.pn[i] = pi;
-        pg += pi * gi;
-        gg += gi * gi;
-        m = nanmax(m, fabs(gi));
-      }
-      const double spg = block_sum(pg, sh), sgg = block_sum(gg, sh), gn1 = block_max(m, sh);
-      if (gn1 <= a.gtol || spg <= -0.01 * sgg) {
+      const double r = v[1] / S.delta;
+      const double beta = r > 0.0 ? r : 0.0;
+      // p1 = -g1 + beta p: p1.g1 = -g1.g1 + beta g1.p
+      const double pg = -v[2] + beta * v[0];
+      if (v[3] <= a.gtol || pg <= -0.01 * v[2]) {
         for (int i = tid; i < a.nv; i += kStepThreads) {
           a.x[i] = a.xt[i];
+          a.p[i] = -a.gt[i] + beta * a.p[i];
           a.g[i] = a.gt[i];
-          a.p[i] = a.pn[i];
         }
         if (tid == 0) {
           S.f_prev = S.f;
           S.f = E;
-          S.gnorm = gn1;
+          S.gnorm = v[3];
+          S.delta = v[2];
+          S.d0 = pg;
           S.k += 1;
           S.restarted = 0;
         }
@@ -664,7 +678,10 @@ __global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cu
       } else {
         for (int i = tid; i < a.nv; i += kStepThreads) a.p[i] = -a.g[i];
         __syncthreads();
-        if (tid == 0) S.restarted = 1;
+        if (tid == 0) {
+          S.restarted = 1;
+          S.d0 = -S.delta;  // p = -g
+        }
         act = A_BEGIN;
       }
       __syncthreads();
@@ -673,14 +690,8 @@ __global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cu
       if (!(S.gnorm > a.gtol) || S.k >= a.maxiter) {
         act = A_STOP_OK;
       } else {
-        double gg = 0.0, gp = 0.0;
-        for (int i = tid; i < a.nv; i += kStepThreads) {
-          gg += a.g[i] * a.g[i];
-          gp += a.g[i] * a.p[i];
-        }
-        const double delta = block_sum(gg, sh), d0 = block_sum(gp, sh);
         if (tid == 0) {
-          S.delta = delta;
+          const double d0 = S.d0;
           double alpha1 = 1.0;
           if (d0 != 0.0) {
             const double v = 1.01 * 2 * (S.f - S.f_prev) / d0;
@@ -780,10 +791,11 @@ void occ_layout(Cv& c, int P, int ndoc, int ncwo, OccState** state, OccArgs& a) 
   a.ns = c.template take<double>(ndoc);
   a.F = c.template take<double>(ndoc);
   a.dF = c.template take<double>(ndoc);
-  a.part = c.template take<double>((size_t)5 * P * nbc);
-  a.row = c.template take<double>((size_t)5 * P);
+  a.part = c.template take<double>((size_t)4 * P * nbc);
+  a.row = c.template take<double>((size_t)4 * P);
   a.pair_of = c.template take<int>(P);
   a.cls = c.template take<int>(P);
+  a.grp = c.template take<unsigned int>((P + 31) / 32);
   a.nv = nv;
   a.nbc = nbc;
 }
@@ -795,11 +807,11 @@ struct OccGraph {
 };
 
 std::mutex g_mu;
-// (context id, workspace) -> graph; a context re-created after
+// (context id, workspace, nbf5) -> graph; a context re-created after
 // cudaDeviceReset has a new id, so a stale graph is never reused
-std::map<std::pair<unsigned long long, const void*>, OccGraph> g_graphs;
+std::map<std::tuple<unsigned long long, const void*, int>, OccGraph> g_graphs;
 
-int build_graph(OccState* st, OccGraph& og) {
+int build_graph(OccState* st, int P, OccGraph& og) {
   cudaGraph_t g = nullptr;
   GB_TRY(gb::cuda_status(cudaGraphCreate(&g, 0), "occ graph create"));
   auto fail = [&](cudaError_t e, const char* where) {
@@ -813,8 +825,7 @@ int build_graph(OccState* st, OccGraph& og) {
   kp.gridDim = dim3(1);
   kp.blockDim = dim3(kStepThreads);
   kp.kernelParams = ip;
-  cudaGraphNode_t init = nullptr, wn = nullptr, n1 = nullptr, n2 = nullptr, n3 = nullptr, n4 = nullptr,
-                  n5 = nullptr;
+  cudaGraphNode_t init = nullptr, wn = nullptr, n4 = nullptr, n5 = nullptr;
   cudaError_t e = cudaGraphAddKernelNode(&init, g, nullptr, 0, &kp);
   if (e != cudaSuccess) return fail(e, "occ graph: init node");
   cudaGraphConditionalHandle h;
@@ -832,25 +843,25 @@ int build_graph(OccState* st, OccGraph& og) {
   void* hp[] = {&st, &h};
   cudaKernelNodeParams r{};
   r.func = (void*)occ_rows_kernel;
-  r.gridDim = dim3(kRowCtas);
+  // one warp per item (the kernel strides over items beyond kRowCtas)
+  const int items = ((P + 31) / 32) * ((P + kBch - 1) / kBch);
+  r.gridDim = dim3(items < kRowCtas ? items : kRowCtas);
   r.blockDim = dim3(32);
   r.kernelParams = sp;
-  e = cudaGraphAddKernelNode(&n1, body, nullptr, 0, &r);
-  if (e != cudaSuccess) return fail(e, "occ graph: rows node");
-  cudaKernelNodeParams rd{};
-  rd.func = (void*)occ_reduce_kernel;
-  rd.gridDim = dim3(kRedCtas);
-  rd.blockDim = dim3(32);
-  rd.kernelParams = sp;
-  e = cudaGraphAddKernelNode(&n2, body, &n1, 1, &rd);
-  if (e != cudaSuccess) return fail(e, "occ graph: reduce node");
   cudaKernelNodeParams sk{};
   sk.func = (void*)occ_step_kernel;
   sk.gridDim = dim3(1);
   sk.blockDim = dim3(kStepThreads);
   sk.kernelParams = hp;
-  e = cudaGraphAddKernelNode(&n3, body, &n2, 1, &sk);
-  if (e != cudaSuccess) return fail(e, "occ graph: step node");
+  cudaGraphNode_t prev = nullptr;
+  for (int u = 0; u < kUnroll; ++u) {
+    cudaGraphNode_t n1 = nullptr, n2 = nullptr;
+    e = cudaGraphAddKernelNode(&n1, body, prev ? &prev : nullptr, prev ? 1 : 0, &r);
+    if (e != cudaSuccess) return fail(e, "occ graph: rows node");
+    e = cudaGraphAddKernelNode(&n2, body, &n1, 1, &sk);
+    if (e != cudaSuccess) return fail(e, "occ graph: step node");
+    prev = n2;
+  }
   cudaKernelNodeParams fk{};
   fk.func = (void*)occ_final_kernel;
   fk.gridDim = dim3(1);
@@ -919,11 +930,11 @@ int occ_run(const double* gamma0, const double* J, const double* K, const double
   a.mode = mode;
   a.gtol = gtol;
   std::lock_guard<std::mutex> lk(g_mu);
-  const auto key = std::make_pair(gb::current_context_id(), (const void*)ws);
+  const auto key = std::make_tuple(gb::current_context_id(), (const void*)ws, nbf5);
   auto it = g_graphs.find(key);
   if (it == g_graphs.end()) {
     OccGraph og;
-    GB_TRY(build_graph(st, og));
+    GB_TRY(build_graph(st, nbf5, og));
     it = g_graphs.emplace(key, og).first;
   }
   void* ip[] = {&st, &a};
@@ -969,7 +980,7 @@ extern "C" int gb_occ_release(const void* ws) {
   gb::clear_error();
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto it = g_graphs.begin(); it != g_graphs.end();) {
-    if (it->first.second == ws) {
+    if (std::get<1>(it->first) == ws) {
       cudaGraphExecDestroy(it->second.exec);
       cudaGraphDestroy(it->second.graph);
       it = g_graphs.erase(it);
