@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--maxit", type=int, default=200)
     ap.add_argument("--time-limit", type=float, default=None, help="seconds per served solve (serve mode)")
     ap.add_argument("--occ-nbf", default="60,300,600", help="nbf of the occupation problems (occ mode)")
+    ap.add_argument("--occupations", choices=["host", "device"], default="host",
+                    help="where served solves run the occupation CG (serve mode)")
     return ap.parse_args()
 
 
@@ -569,7 +571,8 @@ def run_serve(args):
     out = {}
     for prec in ("mixed", "fp64"):
         srv = serve.Server(hbm_budget=150e9, slots=args.slots, precision=prec, nslices=args.nslices,
-                           tol=args.tol, maxit=args.maxit, final_fp64=True, time_limit=args.time_limit)
+                           tol=args.tol, maxit=args.maxit, final_fp64=True, time_limit=args.time_limit,
+                           occupations=args.occupations)
         out[prec] = srv.run(reqs)
         out[prec]["energies"] = {r.rid: r.E_elec for r in srv.results if r.converged}
     both = [k for k in out["fp64"]["energies"] if k in out["mixed"]["energies"]]
@@ -582,6 +585,7 @@ def run_serve(args):
                        "nbf": f"log-uniform {args.nbf_min}..{args.nbf_max}",
                        "naux": "4 nbf", "tol": args.tol, "maxit": args.maxit, "slots": args.slots,
                        "hbm_budget_gb": 150, "time_limit_per_solve_s": args.time_limit,
+                       "occupation_cg": args.occupations,
                        "precision_switch": "six digit slices (FP64-class) throughout; closing Lagrangian "
                                            "(reported energy) on the FP64 path"},
             "mixed": out["mixed"], "plain_fp64": out["fp64"],

@@ -57,7 +57,8 @@
 
 namespace {
 
-constexpr int kStepThreads = 256;
+constexpr int kStepThreads = 256;  // one-CTA kernels
+constexpr int kMinBlocks = 1;
 constexpr int kRowCtas = 4 * 152;  // rows kernel: one warp per CTA, grid-stride over items
 constexpr int kUnroll = 4;         // evaluations per round of the WHILE node
 constexpr int kCjckCtas = 2 * 152;
@@ -504,7 +505,7 @@ __device__ int ls_step(OccState& S, double f, double g) {
 }
 
 // ---- kernels
-__global__ void __launch_bounds__(kStepThreads) occ_init_kernel(OccState* st, OccArgs args) {
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_init_kernel(OccState* st, OccArgs args) {
   OccState& S = *st;
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -561,7 +562,7 @@ __device__ __forceinline__ void copy_state(OccState* dst, const OccState* src) {
 
 __device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h);
 
-__global__ void __launch_bounds__(kStepThreads) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h) {
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h) {
   __shared__ double sh[72];
   __shared__ int s_act;
   // the step works on a copy in shared memory: its scalars and the array
@@ -722,7 +723,7 @@ __device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditio
 }
 
 // the occupations at the result (one CTA), then C^J, C^K (grid)
-__global__ void __launch_bounds__(kStepThreads) occ_final_kernel(const OccState* __restrict__ st) {
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_final_kernel(const OccState* __restrict__ st) {
   const OccArgs& a = st->a;
   if (!a.n_out && !a.cj_out) return;
   prep_point(a, a.x);
@@ -735,7 +736,7 @@ __global__ void __launch_bounds__(kStepThreads) occ_final_kernel(const OccState*
 // +-nd12 nd12^T - nd nd^T terms; inside each pair block C^J = 0 and
 // C^K = sqrt(n_s n_w) (strong-weak), -sqrt(n_w n_w') (weak-weak).  The
 // elementwise order of the numpy expressions, without contraction.
-__global__ void __launch_bounds__(256) occ_cjck_kernel(const OccState* __restrict__ st) {
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_cjck_kernel(const OccState* __restrict__ st) {
   const OccArgs& a = st->a;
   if (!a.cj_out || !a.ck_out) return;
   const int P = a.P, nb = a.no1 + a.ndoc, na = nb;
@@ -872,7 +873,7 @@ int build_graph(OccState* st, int P, OccGraph& og) {
   cudaKernelNodeParams ck{};
   ck.func = (void*)occ_cjck_kernel;
   ck.gridDim = dim3(kCjckCtas);
-  ck.blockDim = dim3(256);
+  ck.blockDim = dim3(kStepThreads);
   ck.kernelParams = sp;
   e = cudaGraphAddKernelNode(&n5, g, &n4, 1, &ck);
   if (e != cudaSuccess) return fail(e, "occ graph: cjck node");

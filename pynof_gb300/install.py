@@ -5,12 +5,13 @@ time (``pynof.computeJKj``, ``pynof.integrals.JKj_RI_GPU``, ...), so
 rebinding those attributes makes every caller -- ``compute_energy``,
 ``occoptr``, ``orbopt_adam``, ``calcorbe`` / ``calcorbg``, ``hfidr`` -- use the
 CUDA kernels when ``p.gpu`` is set, with ``param`` and every signature
-unchanged.  The dispatchers keep the reference's CPU branches for
+unchanged; ``occoptr`` itself becomes the device occupation optimiser for the
+structures it covers.  The dispatchers keep the reference's CPU branches for
 ``p.gpu = False``.
 """
 from __future__ import annotations
 
-from . import integrals, integrals_full, integrals_hf, nof, utils
+from . import integrals, integrals_full, integrals_hf, minimization, nof, utils
 
 #: (module attribute path in pynof, replacement) for the p.gpu branches
 GPU_FUNCTIONS = {
@@ -61,6 +62,19 @@ def _occ_dispatch(cpu_fn, grad: bool):
     fn.__doc__ = (f"p.gpu, GNOF, softmax, closed shell -> the compiled occupation function, "
                   f"else the reference's {fn.__name__}")
     return fn
+
+
+def _occoptr_dispatch(cpu_fn):
+    """occoptr (minimization.py:77-97): the device optimiser where it
+    applies (GNOF, softmax, closed shell, CG, p.gpu), else the reference's."""
+
+    def occoptr(gamma, C, H, I, b_mnl, p):
+        if minimization.device_ok(p):
+            return minimization.occoptr(gamma, C, H, I, b_mnl, p)
+        return cpu_fn(gamma, C, H, I, b_mnl, p)
+
+    occoptr.__doc__ = "p.gpu, GNOF, softmax, closed shell, CG -> the device occupation optimiser, else the reference's occoptr"
+    return occoptr
 
 
 def install(pynof) -> dict:
@@ -123,6 +137,15 @@ def install(pynof) -> dict:
             disp = _occ_dispatch(cpu_fn, grad)
             setattr(pynof.pnof, name, disp)
             setattr(pynof, name, disp)
+    # the occupation optimiser itself (compute_energy calls pynof.occoptr,
+    # energy.py:94, 126)
+    if hasattr(pynof, "minimization") and hasattr(pynof.minimization, "occoptr"):
+        cpu_fn = pynof.minimization.occoptr
+        saved["minimization.occoptr"] = cpu_fn
+        saved["pynof.occoptr"] = getattr(pynof, "occoptr", cpu_fn)
+        disp = _occoptr_dispatch(cpu_fn)
+        pynof.minimization.occoptr = disp
+        pynof.occoptr = disp
     return saved
 
 

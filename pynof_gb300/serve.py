@@ -83,11 +83,20 @@ class Server:
     path, ``final_fp64``); ``fp64_switch`` or ``ladder`` (see
     :func:`pynof_gb300.solver.solve`) switch precision up as the orbital
     gradient falls.  precision "fp64": the plain DMMA path throughout.
-    ``time_limit`` bounds each solve (seconds of its own wall time)."""
+    ``time_limit`` bounds each solve (seconds of its own wall time).
+
+    ``occupations`` chooses where each solve's occupation CG runs.  "host"
+    (the default here) is scipy's CG over the compiled evaluation, which
+    releases the GIL, on the host cores the saturated GPU leaves idle.  On a
+    config-5 stream (6 concurrent solves) it served 10.2 orbital steps/s
+    against 6.0-6.3 with the device graph, whose thousands of small launches
+    per minimisation compete with the other requests' GEMMs.  "device" is
+    :class:`ops.OccMinimizer`, the default of a single solve."""
 
     def __init__(self, hbm_budget: float = 150e9, slots: int = 8, precision: str = "mixed", nslices: int = 6,
                  fp64_switch: float | None = None, tol: float = 1e-5, maxit: int = 200, device=None,
-                 ladder=None, final_fp64: bool = True, time_limit: float | None = None):
+                 ladder=None, final_fp64: bool = True, time_limit: float | None = None,
+                 occupations: str = "host"):
         self.budget = int(hbm_budget)
         self.slots = slots
         self.precision = precision
@@ -96,6 +105,7 @@ class Server:
         self.ladder = ladder if precision == "mixed" else None
         self.final_fp64 = final_fp64 and precision == "mixed"
         self.time_limit = time_limit
+        self.occupations = occupations
         self.tol = tol
         self.maxit = maxit
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -119,7 +129,8 @@ class Server:
         torch.cuda.set_device(self.device)
         st = synthetic.Structure.for_nbf(req.nbf)
         b, C, H, _ = synthetic.make_inputs(st, req.seed)
-        be = solver.Backend(st, b, H, precision=self.precision, nslices=self.nslices, device=self.device)
+        be = solver.Backend(st, b, H, precision=self.precision, nslices=self.nslices, device=self.device,
+                            occupations=self.occupations)
         res = solver.solve(be, C, nof.gamma_guess_softmax(st), st, tol=self.tol, maxit=self.maxit,
                            fp64_switch=self.fp64_switch, ladder=self.ladder, final_fp64=self.final_fp64,
                            time_limit=self.time_limit)

@@ -179,3 +179,27 @@ def test_minimize_edge_cases(torch_cuda):
     assert r[3] == 0.0 and r[2] == 1
     om.close()
     om2.close()
+
+
+@pytest.mark.parametrize("case", ["water", "ragged"])
+def test_dropin_occoptr(torch_cuda, case):
+    """``minimization.occoptr`` (what the installer binds to ``pynof.occoptr``)
+    against the reference's occoptr restated on the host: the oracle's J_MO,
+    K_MO, H_core, scipy's CG over calcocce / calcoccg, then the occupations
+    and CJCKD8 at the result (minimization.py:77-97)."""
+    import scipy.optimize
+
+    from oracle import pynof_oracle as orc
+    from pynof_gb300 import minimization, nof, ops
+
+    g = load_golden(case)
+    p = param_for(case)
+    J, K, Hc = orc.jkh_mo_ri(g["C"], g["H"], g["b"], p.nbf5)
+    ref = scipy.optimize.minimize(nof.calcocce, g["gamma"], args=(J, K, Hc, p), jac=nof.calcoccg, method="CG")
+    E, nit, ok, gam, n, cj, ck = minimization.occoptr(g["gamma"], g["C"], g["H"], None, ops.to_device(g["b"]), p)
+    assert ok and ref.success and nit > 0
+    assert abs(E - ref.fun) <= 1e-10 * abs(ref.fun)
+    assert nrel(gam, ref.x) < 1e-5
+    n_ref, _ = nof.ocupacion_softmax(ref.x, p)
+    cj_ref, ck_ref = nof.cjckd8(n_ref, p)
+    assert nrel(n, n_ref) < 1e-6 and nrel(cj, cj_ref) < 1e-6 and nrel(ck, ck_ref) < 1e-6

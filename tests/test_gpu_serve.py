@@ -14,17 +14,20 @@ def torch_cuda():
     return torch
 
 
-def test_alone_equals_in_mix(torch_cuda):
+@pytest.mark.parametrize("occupations", ["host", "device"])
+def test_alone_equals_in_mix(torch_cuda, occupations):
+    """With the occupation CG on the host or as each request's own device
+    graph (its own workspace, fixed-order reductions)."""
     from pynof_gb300 import serve
 
     reqs = serve.poisson_stream(6, rate=200.0, nbf_lo=24, nbf_hi=48, seed=5)
-    mixed = serve.Server(slots=4, tol=1e-4, maxit=60)
+    mixed = serve.Server(slots=4, tol=1e-4, maxit=60, occupations=occupations)
     rep = mixed.run(reqs)
     assert rep["completed"] == 6 and rep["failed"] == 0, mixed.errors
     assert rep["peak_active"] > 1  # requests were on the GPU together
     in_mix = {r.rid: r.E_elec for r in mixed.results}
     for req in reqs[:3]:
-        alone = serve.Server(slots=1, tol=1e-4, maxit=60)
+        alone = serve.Server(slots=1, tol=1e-4, maxit=60, occupations=occupations)
         rep1 = alone.run([serve.Request(req.rid, req.nbf, req.seed, 0.0)])
         assert rep1["completed"] == 1
         assert alone.results[0].E_elec == in_mix[req.rid]

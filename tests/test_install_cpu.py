@@ -34,7 +34,30 @@ def fake_pynof():
     pynof.pnof.calcoccg = lambda *a: ("reference", "calcoccg")
     pynof.calcocce = pynof.pnof.calcocce
     pynof.calcoccg = pynof.pnof.calcoccg
+    pynof.minimization = types.ModuleType("pynof.minimization")
+    pynof.minimization.occoptr = lambda *a: ("reference", "occoptr")
+    pynof.occoptr = pynof.minimization.occoptr
     return pynof
+
+
+def test_install_occoptr_dispatch():
+    """occoptr becomes the device optimiser's dispatcher; structures it does
+    not cover (and p.gpu = False) reach the reference's own occoptr."""
+    from pynof_gb300 import minimization, synthetic
+
+    pynof = fake_pynof()
+    orig = pynof.occoptr
+    saved = inst.install(pynof)
+    assert pynof.occoptr is pynof.minimization.occoptr and pynof.occoptr is not orig
+    st = synthetic.structure("water")
+    assert minimization.device_ok(st)
+    for other in (dict(gpu=False), dict(ipnof=7), dict(occ_method="Trigonometric"),
+                  dict(occupation_optimizer="L-BFGS-B"), dict(freeze_occ=True), dict(MSpin=1)):
+        q = types.SimpleNamespace(**{**vars(st), **other})
+        assert not minimization.device_ok(q)
+        assert pynof.occoptr(None, None, None, None, None, q) == ("reference", "occoptr")
+    inst.uninstall(pynof, saved)
+    assert pynof.occoptr is orig and pynof.minimization.occoptr is orig
 
 
 def test_install_occupation_function():

@@ -10,6 +10,8 @@ and the import path stay out of this test session).  After
   ``computeF_RC_driver``, ``compute_energy``'s callees) resolve it through
   their module globals -- the lookup PyNOF makes at call time;
 * the names re-exported at the package top level point at the same objects;
+* ``occoptr``, which ``compute_energy`` calls as ``pynof.occoptr``, becomes
+  the device occupation optimiser's dispatcher;
 * the p.gpu=False branches of the replaced-whole functions
   (``computeLagrange2``, ``calcocce``) still return the reference's CPU
   results on the golden inputs;
@@ -80,6 +82,9 @@ for name in ("computeLagrange2", "ENERGY1r", "rotate_orbital"):
     out["toplevel"][name] = getattr(pynof, name, getattr(pynof.utils, name)) is getattr(pynof.utils, name)
 for name in ("calcocce", "calcoccg"):
     out["resolved"]["pnof." + name] = "compiled occupation function" in getattr(pynof.pnof, name).__doc__
+# compute_energy calls pynof.occoptr (energy.py:94, 126)
+out["resolved"]["occoptr"] = (pynof.occoptr is pynof.minimization.occoptr
+                              and "device occupation optimiser" in pynof.occoptr.__doc__)
 # p.gpu = False: the reference's CPU branches behind the dispatchers
 z = np.load(GOLDEN + "/c1.npz")
 from pynof_gb300 import synthetic
@@ -93,6 +98,7 @@ out["cpu"]["calcocce"] = abs(float(E) - float(z["E_calcocce"])) / abs(float(z["E
 install.uninstall(pynof, saved)
 out["restored"] = all(getattr(getattr(pynof, d.split(".")[0]), d.split(".")[1]) is f for d, f in before.items())
 out["restored_lagrange2"] = not (pynof.utils.computeLagrange2.__doc__ or "").startswith("p.gpu -> pynof_gb300")
+out["restored_occoptr"] = "device occupation optimiser" not in (pynof.occoptr.__doc__ or "")
 print("RESULT " + json.dumps(out))
 """
 
@@ -110,4 +116,4 @@ def test_install_on_reference_package(tmp_path):
     assert all(out["resolved"].values()), out["resolved"]
     assert all(out["toplevel"].values()), out["toplevel"]
     assert out["cpu"]["computeLagrange2"] < 1e-12 and out["cpu"]["calcocce"] < 1e-12, out["cpu"]
-    assert out["restored"] and out["restored_lagrange2"]
+    assert out["restored"] and out["restored_lagrange2"] and out["restored_occoptr"]
