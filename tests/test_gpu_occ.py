@@ -4,7 +4,8 @@ gb_occ_energy_grad_dev) against the host evaluation and scipy's CG.
 * one evaluation E(gamma), dE/dgamma against the compiled host loop
   (gb_occ_energy_grad_f64, itself pinned to the reference's calcocce /
   calcoccg golden values) on the golden problems, a synthetic one from the
-  oracle's J_MO / K_MO, an nbf5 = 300 problem and logits past exp's range;
+  oracle's J_MO / K_MO, an nbf5 = 300 problem, inactive core orbitals
+  (no1 > 0), one weak orbital per pair, and logits past exp's range;
 * the whole minimisation against scipy's CG on the host (the reference's
   optimiser, ``pynof/minimization.py:77-97``): same minimum (energy to
   1e-12 relative, gamma to 1e-6), converged to gtol;
@@ -45,9 +46,15 @@ def _problem(case):
         b, C, H, _ = synthetic.make_inputs(st, seed=1)
         J, K, Hc = orc.jkh_mo_ri(C, H, b, st.nbf5)
         return st, nof.gamma_guess_softmax(st), J, K, Hc
-    # nbf5 = 300 (the nbf=600 structure): symmetric positive J, K with a
-    # dominant diagonal, H_core spread over the orbitals
-    st = synthetic.structure("c3")
+    if case in ("no1", "ncwo1"):
+        # inactive core orbitals (no1 > 0), or one weak orbital per pair
+        st = synthetic.Structure(nbf=40, nbfaux=160, ndoc=4, ncwo=3, no1=2) if case == "no1" else \
+            synthetic.Structure(nbf=40, nbfaux=160, ndoc=6, ncwo=1)
+    else:
+        # nbf5 = 300 (the nbf=600 structure)
+        st = synthetic.structure("c3")
+    # symmetric positive J, K with a dominant diagonal, H_core spread over
+    # the orbitals
     P = st.nbf5
     rng = np.random.default_rng(5)
     A = 0.01 * rng.standard_normal((P, P))
@@ -64,7 +71,7 @@ def _dev(*xs):
     return [ops.to_device(np.ascontiguousarray(x, dtype=np.float64)) for x in xs]
 
 
-CASES = ["c1", "water", "ragged", "syn120", "p300"]
+CASES = ["c1", "water", "ragged", "syn120", "p300", "no1", "ncwo1"]
 
 
 @pytest.mark.parametrize("case", CASES)
