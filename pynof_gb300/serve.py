@@ -118,11 +118,19 @@ class Server:
         self.results: list[Result] = []
         self.errors: list[tuple[int, str]] = []
         self.steps = 0  # orbital steps (device Lagrangian evaluations) of finished solves
+        # summed over finished solves: seconds in the occupation CG and in the
+        # orbital-step loops, and the CG iterations
+        self.t_occ = 0.0
+        self.t_orb = 0.0
+        self.cg_iterations = 0
         self.solve_fn = self.solve_request
 
-    def _note_steps(self, k: int):
+    def _note_steps(self, k: int, t_occ: float = 0.0, t_orb: float = 0.0, cg_iterations: int = 0):
         with self._lock:
             self.steps += k
+            self.t_occ += t_occ
+            self.t_orb += t_orb
+            self.cg_iterations += cg_iterations
 
     def solve_request(self, req: Request):
         """Full NOF solve of one request on its own stream: (E, converged, iterations)."""
@@ -135,7 +143,8 @@ class Server:
                            fp64_switch=self.fp64_switch, ladder=self.ladder, final_fp64=self.final_fp64,
                            time_limit=self.time_limit)
         be.stream.synchronize()
-        self._note_steps(be.calls["lagrange2"])
+        self._note_steps(be.calls["lagrange2"], res.history["t_occ"], res.history["t_orb"],
+                         int(np.sum(res.history["nit_occ"])))
         return res.E_elec, res.converged, res.iterations
 
     # ---- one solve -----------------------------------------------------
@@ -204,6 +213,8 @@ class Server:
             "p50_latency_converged_s": float(np.percentile(clat, 50)),
             "p99_latency_converged_s": float(np.percentile(clat, 99)),
             "orbital_steps_per_s": self.steps / wall,
+            "occupation_cg_s": self.t_occ, "orbital_loops_s": self.t_orb, "occupation_cg_iterations": self.cg_iterations,
+            "occupations": self.occupations,
             "peak_active": self.peak_active, "peak_reserved_gb": self.peak_reserved / 1e9,
             "precision": self.precision, "slots": self.slots, "budget_gb": self.budget / 1e9,
             "time_limit_s": self.time_limit,

@@ -355,15 +355,24 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
     p = copy.copy(p)
     state = SolveState(alpha=getattr(p, "alpha", 0.02), maxloop=getattr(p, "maxloop", 30))
     hist = {k: [] for k in ("E_orb", "E_occ", "g_orb", "g_occ", "nit_orb", "nit_occ", "precision")}
+    # wall time of the occupation CG and of the orbital steps (seconds)
+    hist["t_occ"] = 0.0
+    hist["t_orb"] = 0.0
+    t = time.perf_counter()
     E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
+    hist["t_occ"] += time.perf_counter() - t
     hist["E_occ"].append(E_occ)
     hist["nit_occ"].append(nit_occ)
     converged = False
     it = 0
     deadline = None if time_limit is None else t0 + time_limit
     for it in range(maxit):
+        t = time.perf_counter()
         E_orb, C, nit_orb, ok_orb = orbopt_adam(gamma, C, be, p, state, deadline=deadline)
+        t1 = time.perf_counter()
         E_occ, nit_occ, ok_occ, gamma, n, cj12, ck12 = occoptr(gamma, C, be, p)
+        hist["t_orb"] += t1 - t
+        hist["t_occ"] += time.perf_counter() - t1
         C, gamma = nof.order_occupations_softmax(C, gamma, p)
         g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
         if p.ndoc > 0 and getattr(be, "occupations", "host") == "device" and nof.native_occ_ok(p):
