@@ -279,6 +279,15 @@ int gb_occ_minimize_dev(const double* gamma0, const double* J_MO, const double* 
                         int nbf5, int no1, int ndoc, int ncwo, double gtol, int maxiter, double* gamma_out,
                         double* result, double* n_out, double* cj12_out, double* ck12_out, void* ws,
                         size_t ws_bytes, void* stream);
+/* gb_occ_minimize_dev driven from the host: the same kernels and steps, as
+ * replays of an ordinary graph of eight evaluations with the phase copied back
+ * (one synchronisation of `stream` per replay) instead of the conditional
+ * node; returns when the minimisation has ended (GB_ERR_TIMEOUT if it did not
+ * within the evaluation cap). */
+int gb_occ_minimize_dev_sync(const double* gamma0, const double* J_MO, const double* K_MO, const double* H_core,
+                             int nbf5, int no1, int ndoc, int ncwo, double gtol, int maxiter, double* gamma_out,
+                             double* result, double* n_out, double* cj12_out, double* ck12_out, void* ws,
+                             size_t ws_bytes, void* stream);
 /* One evaluation of E(gamma) and dE/dgamma on the device (calcocce +
  * calcoccg, pnof.py:994-1033): result[0] = E, result[4] = ||g||_inf, grad
  * [ndoc ncwo] (may be null); same workspace as gb_occ_minimize_dev. */

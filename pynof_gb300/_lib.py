@@ -78,6 +78,8 @@ SIGNATURES = {
     "gb_calce_f64": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
     "gb_occ_workspace_bytes": (_Z, [_I, _I, _I]),
     "gb_occ_minimize_dev": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _c.c_double, _I, _P, _P, _P, _P, _P, _P, _Z, _P]),
+    "gb_occ_minimize_dev_sync": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _c.c_double, _I, _P, _P, _P, _P, _P, _P, _Z,
+                                      _P]),
     "gb_occ_energy_grad_dev": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _Z, _P]),
     "gb_occ_release": (_I, [_P]),
     "gb_device_status": (_I, [_I, _c.POINTER(_I)]),

@@ -43,12 +43,15 @@
 // kernel clears the condition when the minimiser stops and the kernels after
 // it return at once), then the occupations and C^J, C^K at the result.  The
 // number of evaluations is capped at 1 + 200 (maxiter + 1): a minimiser that
-// reaches the cap reports success -1.
+// reaches the cap reports success -1.  The host-driven form
+// (gb_occ_minimize_dev_sync) replays an ordinary graph of eight rounds instead
+// of the conditional node and reads the phase back after each replay.
 //
 // All arithmetic is FP64 (GB300's FP64 rate is low, so the O(nbf5^2) pair
 // work is spread over the whole GPU and the single-CTA work is O(nbf5)).
 // Closed shell without singly occupied orbitals (MSpin = 0, nsoc = 0).
 #include <cmath>
+#include <cstddef>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -538,7 +541,7 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_init_kernel(OccS
   prep_point(a, a.xt);
 }
 
-__device__ void finish(OccState& S, double success, cudaGraphConditionalHandle h) {
+__device__ void finish(OccState& S, double success, cudaGraphConditionalHandle h, int cond) {
   const OccArgs& a = S.a;
   for (int i = threadIdx.x; i < a.nv; i += kStepThreads) a.gamma_out[i] = a.x[i];
   if (threadIdx.x == 0) {
@@ -548,7 +551,7 @@ __device__ void finish(OccState& S, double success, cudaGraphConditionalHandle h
     a.res[3] = success;
     a.res[4] = S.gnorm;
     S.phase = PH_DONE;
-    cudaGraphSetConditional(h, 0);
+    if (cond) cudaGraphSetConditional(h, 0);
   }
 }
 
@@ -560,26 +563,26 @@ __device__ __forceinline__ void copy_state(OccState* dst, const OccState* src) {
   for (int i = threadIdx.x; i < (int)(sizeof(OccState) / 8); i += blockDim.x) d[i] = s[i];
 }
 
-__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h);
+__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h, int cond);
 
-__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h) {
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks) occ_step_kernel(OccState* st, cudaGraphConditionalHandle h, int cond) {
   __shared__ double sh[72];
   __shared__ int s_act;
   // the step works on a copy in shared memory: its scalars and the array
   // pointers are read there, not from global memory behind every store
   __shared__ OccState S;
   if (st->phase == PH_DONE) {
-    if (threadIdx.x == 0) cudaGraphSetConditional(h, 0);
+    if (threadIdx.x == 0 && cond) cudaGraphSetConditional(h, 0);
     return;
   }
   copy_state(&S, st);
   __syncthreads();
-  step_body(S, sh, s_act, h);
+  step_body(S, sh, s_act, h, cond);
   __syncthreads();
   copy_state(st, &S);
 }
 
-__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h) {
+__device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditionalHandle h, int cond) {
   const OccArgs& a = S.a;
   const int tid = threadIdx.x;
   const double E = assemble(a, sh);
@@ -597,7 +600,7 @@ __device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditio
       S.gnorm = v[0];
     }
     __syncthreads();
-    finish(S, 1.0, h);
+    finish(S, 1.0, h, cond);
     return;
   }
   enum { A_BEGIN, A_FAIL, A_EVAL, A_STOP_OK, A_STOP_FAIL, A_STOP_CAP };
@@ -719,7 +722,7 @@ __device__ void step_body(OccState& S, double* sh, int& s_act, cudaGraphConditio
   }
   __syncthreads();
   const double success = act == A_STOP_CAP ? -1.0 : (act == A_STOP_OK && S.gnorm <= a.gtol ? 1.0 : 0.0);
-  finish(S, success, h);
+  finish(S, success, h, cond);
 }
 
 // the occupations at the result (one CTA), then C^J, C^K (grid)
@@ -805,7 +808,14 @@ struct OccGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraphNode_t init = nullptr;
+  // host-driven form: kChunk evaluations as an ordinary graph, and a pinned
+  // word the phase is copied into after each replay
+  cudaGraph_t chunk_graph = nullptr;
+  cudaGraphExec_t chunk_exec = nullptr;
+  int* flag = nullptr;
 };
+
+constexpr int kChunk = 8;  // evaluations per replay of the host-driven form
 
 std::mutex g_mu;
 // (context id, workspace, nbf5) -> graph; a context re-created after
@@ -841,7 +851,8 @@ int build_graph(OccState* st, int P, OccGraph& og) {
   if (e != cudaSuccess) return fail(e, "occ graph: while node");
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   void* sp[] = {&st};
-  void* hp[] = {&st, &h};
+  int cond = 1;
+  void* hp[] = {&st, &h, &cond};
   cudaKernelNodeParams r{};
   r.func = (void*)occ_rows_kernel;
   // one warp per item (the kernel strides over items beyond kRowCtas)
@@ -886,10 +897,84 @@ int build_graph(OccState* st, int P, OccGraph& og) {
   return GB_OK;
 }
 
+// kChunk rounds of rows -> step as an ordinary graph (no conditional node:
+// the kernels return at once after the minimiser stopped)
+int build_chunk_graph(OccState* st, int P, OccGraph& og) {
+  cudaGraph_t g = nullptr;
+  GB_TRY(gb::cuda_status(cudaGraphCreate(&g, 0), "occ chunk graph create"));
+  auto fail = [&](cudaError_t e, const char* where) {
+    cudaGraphDestroy(g);
+    return gb::cuda_status(e, where);
+  };
+  void* sp[] = {&st};
+  cudaGraphConditionalHandle h = 0;
+  int cond = 0;
+  void* hp[] = {&st, &h, &cond};
+  cudaKernelNodeParams r{};
+  r.func = (void*)occ_rows_kernel;
+  const int items = ((P + 31) / 32) * ((P + kBch - 1) / kBch);
+  r.gridDim = dim3(items < kRowCtas ? items : kRowCtas);
+  r.blockDim = dim3(32);
+  r.kernelParams = sp;
+  cudaKernelNodeParams sk{};
+  sk.func = (void*)occ_step_kernel;
+  sk.gridDim = dim3(1);
+  sk.blockDim = dim3(kStepThreads);
+  sk.kernelParams = hp;
+  cudaGraphNode_t prev = nullptr;
+  for (int u = 0; u < kChunk; ++u) {
+    cudaGraphNode_t n1 = nullptr, n2 = nullptr;
+    cudaError_t e = cudaGraphAddKernelNode(&n1, g, prev ? &prev : nullptr, prev ? 1 : 0, &r);
+    if (e != cudaSuccess) return fail(e, "occ chunk graph: rows node");
+    e = cudaGraphAddKernelNode(&n2, g, &n1, 1, &sk);
+    if (e != cudaSuccess) return fail(e, "occ chunk graph: step node");
+    prev = n2;
+  }
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  if (e != cudaSuccess) return fail(e, "occ chunk graph: instantiate");
+  int* flag = nullptr;
+  e = cudaHostAlloc(&flag, sizeof(int), cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGraphExecDestroy(exec);
+    return fail(e, "occ chunk graph: pinned flag");
+  }
+  og.chunk_graph = g;
+  og.chunk_exec = exec;
+  og.flag = flag;
+  return GB_OK;
+}
+
+// The host-driven minimisation: init, then replays of the chunk graph until
+// the phase copied back reads done (at most the evaluation cap's worth of
+// replays), then the occupations and C^J, C^K.  Synchronises `s` once per
+// replay.
+int run_host_driven(OccState* st, const OccArgs& a, OccGraph& og, cudaStream_t s, const char* name) {
+  occ_init_kernel<<<1, kStepThreads, 0, s>>>(st, a);
+  GB_CHECK_LAUNCH(name);
+  const long long maxev = 1 + 200LL * (a.maxiter + 1);
+  const long long max_replays = maxev / kChunk + 2;
+  int phase = PH_INIT;
+  for (long long r = 0; r < max_replays && phase != PH_DONE; ++r) {
+    GB_TRY(gb::cuda_status(cudaGraphLaunch(og.chunk_exec, s), name));
+    GB_TRY(gb::cuda_status(cudaMemcpyAsync(og.flag, reinterpret_cast<const char*>(st) + offsetof(OccState, phase),
+                                           sizeof(int), cudaMemcpyDeviceToHost, s),
+                           name));
+    GB_TRY(gb::cuda_status(cudaStreamSynchronize(s), name));
+    phase = *og.flag;
+  }
+  GB_REQUIRE(phase == PH_DONE, GB_ERR_TIMEOUT, "%s: the minimiser did not stop within the evaluation cap", name);
+  occ_final_kernel<<<1, kStepThreads, 0, s>>>(st);
+  GB_CHECK_LAUNCH(name);
+  occ_cjck_kernel<<<kCjckCtas, kStepThreads, 0, s>>>(st);
+  GB_CHECK_LAUNCH(name);
+  return GB_OK;
+}
+
 int occ_run(const double* gamma0, const double* J, const double* K, const double* H, int nbf5, int no1, int ndoc,
             int ncwo, double gtol, int maxiter, int mode, double* gamma_out, double* grad_out, double* result,
             double* n_out, double* cj_out, double* ck_out, void* ws, size_t ws_bytes, void* stream,
-            const char* name) {
+            const char* name, bool host_driven = false) {
   gb::clear_error();
   GB_REQUIRE(gamma0 && J && K && H && result && ws, GB_ERR_INVALID_ARG, "%s: null pointer", name);
   GB_REQUIRE(mode == MODE_EVAL || gamma_out, GB_ERR_INVALID_ARG, "%s: null gamma_out", name);
@@ -938,6 +1023,13 @@ int occ_run(const double* gamma0, const double* J, const double* K, const double
     GB_TRY(build_graph(st, nbf5, og));
     it = g_graphs.emplace(key, og).first;
   }
+  if (host_driven) {
+    if (!it->second.chunk_exec) GB_TRY(build_chunk_graph(st, nbf5, it->second));
+    const int pi = gb::prof_begin(name, s);
+    const int rc = run_host_driven(st, a, it->second, s, name);
+    gb::prof_end(pi, s);
+    return rc;
+  }
   void* ip[] = {&st, &a};
   cudaKernelNodeParams kp{};
   kp.func = (void*)occ_init_kernel;
@@ -970,6 +1062,14 @@ extern "C" int gb_occ_minimize_dev(const double* gamma0, const double* J_MO, con
                  result, n_out, cj12_out, ck12_out, ws, ws_bytes, stream, "gb_occ_minimize_dev");
 }
 
+extern "C" int gb_occ_minimize_dev_sync(const double* gamma0, const double* J_MO, const double* K_MO,
+                                        const double* H_core, int nbf5, int no1, int ndoc, int ncwo, double gtol,
+                                        int maxiter, double* gamma_out, double* result, double* n_out,
+                                        double* cj12_out, double* ck12_out, void* ws, size_t ws_bytes, void* stream) {
+  return occ_run(gamma0, J_MO, K_MO, H_core, nbf5, no1, ndoc, ncwo, gtol, maxiter, MODE_MIN, gamma_out, nullptr,
+                 result, n_out, cj12_out, ck12_out, ws, ws_bytes, stream, "gb_occ_minimize_dev_sync", true);
+}
+
 extern "C" int gb_occ_energy_grad_dev(const double* gamma, const double* J_MO, const double* K_MO,
                                       const double* H_core, int nbf5, int no1, int ndoc, int ncwo, double* result,
                                       double* grad, void* ws, size_t ws_bytes, void* stream) {
@@ -984,6 +1084,9 @@ extern "C" int gb_occ_release(const void* ws) {
     if (std::get<1>(it->first) == ws) {
       cudaGraphExecDestroy(it->second.exec);
       cudaGraphDestroy(it->second.graph);
+      if (it->second.chunk_exec) cudaGraphExecDestroy(it->second.chunk_exec);
+      if (it->second.chunk_graph) cudaGraphDestroy(it->second.chunk_graph);
+      if (it->second.flag) cudaFreeHost(it->second.flag);
       it = g_graphs.erase(it);
     } else {
       ++it;

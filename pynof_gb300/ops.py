@@ -397,14 +397,18 @@ class OccMinimizer:
         _require(H, (P,), "H_core")
 
     def minimize(self, gamma0, J_MO, K_MO, H_core, gtol: float = 1e-5, maxiter: int | None = None,
-                 coefficients: bool = True):
+                 coefficients: bool = True, host_driven: bool = False):
         """Launch the minimisation from gamma0; returns the device tensors
         (gamma, result, n, cj12, ck12) it fills (n, cj12, ck12 at the result;
-        None with ``coefficients=False``)."""
+        None with ``coefficients=False``).  ``host_driven`` replays an
+        ordinary graph of eight evaluations and reads the phase back after
+        each (``gb_occ_minimize_dev_sync``; returns when done) instead of the
+        conditional-node graph."""
         self._check(gamma0, J_MO, K_MO, H_core)
         maxiter = 200 * self.nv if maxiter is None else int(maxiter)
         co = (self.n, self.cj12, self.ck12) if coefficients else (None, None, None)
-        _lib.call("gb_occ_minimize_dev", _ptr(gamma0), _ptr(J_MO), _ptr(K_MO), _ptr(H_core), *self.dims,
+        entry = "gb_occ_minimize_dev_sync" if host_driven else "gb_occ_minimize_dev"
+        _lib.call(entry, _ptr(gamma0), _ptr(J_MO), _ptr(K_MO), _ptr(H_core), *self.dims,
                   float(gtol), maxiter, _ptr(self.gamma), _ptr(self.result), *(_ptr(t) for t in co), self._wp,
                   self._wn, _stream(self.device))
         return (self.gamma, self.result) + co

@@ -89,9 +89,9 @@ class Server:
     (the default here) is scipy's CG over the compiled evaluation, which
     releases the GIL, on the host cores the saturated GPU leaves idle.  On a
     config-5 stream (6 concurrent solves) it served 10.2 orbital steps/s
-    against 6.0-6.3 with the device graph, whose thousands of small launches
-    per minimisation compete with the other requests' GEMMs.  "device" is
-    :class:`ops.OccMinimizer`, the default of a single solve."""
+    against 6.3 with the device graph ("device", :class:`ops.OccMinimizer`,
+    the default of a single solve), whose device-side loop slows the other
+    requests' GEMMs, and 6.0 driven from the host ("device_sync")."""
 
     def __init__(self, hbm_budget: float = 150e9, slots: int = 8, precision: str = "mixed", nslices: int = 6,
                  fp64_switch: float | None = None, tol: float = 1e-5, maxit: int = 200, device=None,

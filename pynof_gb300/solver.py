@@ -42,12 +42,14 @@ class Backend:
 
     def __init__(self, st, b, H, precision: str = "mixed", nslices: int = 6, device=None, stream=None,
                  use_graphs: bool = True, occupations: str = "device"):
-        if occupations not in ("device", "host"):
-            raise ValueError(f"occupations must be 'device' or 'host', got {occupations!r}")
+        if occupations not in ("device", "device_sync", "host"):
+            raise ValueError(f"occupations must be 'device', 'device_sync' or 'host', got {occupations!r}")
         self.st = st
         self.use_graphs = use_graphs
-        # "device": occoptr's CG runs on the device (ops.OccMinimizer) at the
-        # device J_MO, K_MO, H_core; "host": scipy's CG over the compiled host
+        # "device": occoptr's CG runs on the device (ops.OccMinimizer, one
+        # conditional-node graph) at the device J_MO, K_MO, H_core;
+        # "device_sync": the same kernels driven from the host in replays of
+        # eight evaluations; "host": scipy's CG over the compiled host
         # evaluation (scipy's own iterates)
         self.occupations = occupations
         self._occ = None
@@ -121,7 +123,8 @@ class Backend:
         with torch.cuda.stream(self.stream):
             J, K, Hc = self._jkh_mo_dev(ops.to_device(C, self.device))
             om = self._occ_min()
-            gam, res, n, cj, ck = om.minimize(ops.to_device(gamma, self.device), J, K, Hc)
+            gam, res, n, cj, ck = om.minimize(ops.to_device(gamma, self.device), J, K, Hc,
+                                              host_driven=self.occupations == "device_sync")
             gam, res, n, cj, ck = self._sync_host(gam, res, n, cj, ck)
         if res[3] < 0:
             raise RuntimeError("occupation minimiser reached its evaluation cap")
@@ -257,7 +260,7 @@ def occoptr(gamma, C, be, p):
     """``minimization.py:77-97``: CG over gamma at fixed orbitals -- on the
     device when the backend's ``occupations`` is "device" (closed shell),
     else scipy's CG over the compiled host evaluation."""
-    if p.ndoc > 0 and getattr(be, "occupations", "host") == "device" and nof.native_occ_ok(p):
+    if p.ndoc > 0 and getattr(be, "occupations", "host") != "host" and nof.native_occ_ok(p):
         return be.occ_minimize(gamma, C)
     J_MO, K_MO, H_core = be.jkh_mo(C)
     E, nit, success = 0.0, 0, True
@@ -375,7 +378,7 @@ def solve(be: Backend, C, gamma, p, tol: float = 1e-3, maxit: int = 1000, fp64_s
         hist["t_occ"] += time.perf_counter() - t1
         C, gamma = nof.order_occupations_softmax(C, gamma, p)
         g_orb = np.linalg.norm(calcorbg(np.zeros(p.nvar), n, cj12, ck12, C, be, p))
-        if p.ndoc > 0 and getattr(be, "occupations", "host") == "device" and nof.native_occ_ok(p):
+        if p.ndoc > 0 and getattr(be, "occupations", "host") != "host" and nof.native_occ_ok(p):
             g_occ = np.linalg.norm(be.occ_gradient(gamma, C))
         else:
             J_MO, K_MO, H_core = be.jkh_mo(C)

@@ -210,3 +210,20 @@ def test_dropin_occoptr(torch_cuda, case):
     n_ref, _ = nof.ocupacion_softmax(ref.x, p)
     cj_ref, ck_ref = nof.cjckd8(n_ref, p)
     assert nrel(n, n_ref) < 1e-6 and nrel(cj, cj_ref) < 1e-6 and nrel(ck, ck_ref) < 1e-6
+
+
+@pytest.mark.parametrize("case", ["c1", "syn120", "p300"])
+def test_host_driven_matches_graph(torch_cuda, case):
+    """gb_occ_minimize_dev_sync (replays of an ordinary graph, the phase read
+    back after each) runs the same kernels and steps as the conditional-node
+    graph: bit-identical gamma, result, n, C^J, C^K."""
+    from pynof_gb300 import ops
+
+    p, g0, J, K, Hc = _problem(case)
+    dg, dJ, dK, dH = _dev(g0, J, K, Hc)
+    om = ops.OccMinimizer(p.nbf5, p.no1, p.ndoc, p.ncwo)
+    a = [t.cpu().numpy().copy() for t in om.minimize(dg, dJ, dK, dH)]
+    b = [t.cpu().numpy().copy() for t in om.minimize(dg, dJ, dK, dH, host_driven=True)]
+    assert b[1][3] == 1.0
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

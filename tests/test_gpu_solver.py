@@ -22,7 +22,7 @@ def torch_cuda():
 
 
 @pytest.mark.parametrize("precision,occupations", [("fp64", "host"), ("mixed", "host"), ("fp64", "device"),
-                                                    ("mixed", "device")])
+                                                    ("mixed", "device"), ("mixed", "device_sync")])
 def test_loop_matches_reference(torch_cuda, precision, occupations):
     """With the occupations on the host the CG takes scipy's own iterates;
     on the device it takes the same steps up to rounding."""
