@@ -277,6 +277,79 @@ def calce(n, cj12, ck12, J_MO, K_MO, H_core, p):
     return E
 
 
+def ocupacion_softmax(x, p):
+    """Occupations n (nbf5,) from the gammas (``pnof.py:770-809``): per pair
+    i, one softmax over a zero logit for the strong orbital and the ncwo weak
+    ones at ll, ll + ndoc, ...; the strong occupation is stored at index i (as
+    the reference does); singly occupied orbitals at 0.5 (1.0 high spin)."""
+    no1, ndoc, ndns, ncwo = p.no1, p.ndoc, p.ndns, p.ncwo
+    n = np.zeros(p.nbf5)
+    n[no1 + ndoc: no1 + ndns] = 1.0 if getattr(p, "HighSpin", False) else 0.5
+    ex = np.exp(np.asarray(x, dtype=np.float64))
+    for i in range(ndoc):
+        ll = no1 + ndns + (ndoc - i - 1)
+        llx = ndoc - i - 1
+        e = ex[llx: llx + ndoc * ncwo: ndoc]
+        den = 1 + np.sum(e)
+        n[i] = 1 / den
+        n[ll: ll + ndoc * ncwo: ndoc] = e / den
+    return n
+
+
+def cjckd8(n, p):
+    """GNOF coefficients C^J, C^K (``pnof.py:350-422``, CJCKD8), MSpin == 0."""
+    no1, ndoc, nsoc, nb, na, ndns, ncwo = p.no1, p.ndoc, p.nsoc, p.nbeta, p.nalpha, p.ndns, p.ncwo
+    h_cut = 0.02 * np.sqrt(2.0)
+    n_d = np.zeros(len(n))
+    for i in range(ndoc):
+        idx = no1 + i
+        ll = no1 + ndns + (ndoc - i - 1)
+        ul = ll + ndoc * ncwo
+        F = np.exp(-(((1.0 - n[idx]) / h_cut) ** 2))
+        n_d[idx] = n[idx] * F
+        n_d[ll:ul:ndoc] = n[ll:ul:ndoc] * F
+    n_d12 = np.sqrt(n_d)
+    fi = n * (1 - n)
+    fi[fi <= 0] = 0
+    fi = np.sqrt(fi)
+    cj12 = 2 * np.outer(n, n)
+    ck12 = np.outer(n, n)
+    ck12[no1:nb, na:] += np.outer(fi[no1:nb], fi[na:])
+    ck12[na:, no1:nb] += np.outer(fi[na:], fi[no1:nb])
+    ck12[na:, na:] += np.outer(fi[na:], fi[na:])
+    if nsoc > 0:
+        half = np.full(nsoc, 0.5)
+        ck12[no1:nb, nb:na] += 0.5 * np.outer(fi[no1:nb], half)
+        ck12[nb:na, no1:nb] += 0.5 * np.outer(half, fi[no1:nb])
+        ck12[nb:na, na:] += np.outer(half, fi[na:])
+        ck12[na:, nb:na] += np.outer(fi[na:], half)
+    if nsoc > 1:
+        ck12[nb:na, nb:na] = 0.5
+    ck12[no1:nb, na:] += np.outer(n_d12[no1:nb], n_d12[na:]) - np.outer(n_d[no1:nb], n_d[na:])
+    ck12[na:, no1:nb] += np.outer(n_d12[na:], n_d12[no1:nb]) - np.outer(n_d[na:], n_d[no1:nb])
+    ck12[na:, na:] += -np.outer(n_d12[na:], n_d12[na:]) - np.outer(n_d[na:], n_d[na:])
+    for i in range(ndoc):
+        idx = no1 + i
+        ll = no1 + ndns + (ndoc - i - 1)
+        ul = ll + ndoc * ncwo
+        nw = n[ll:ul:ndoc]
+        cj12[idx, ll:ul:ndoc] = 0
+        cj12[ll:ul:ndoc, idx] = 0
+        cj12[ll:ul:ndoc, ll:ul:ndoc] = 0
+        ck12[idx, ll:ul:ndoc] = np.sqrt(n[idx] * nw)
+        ck12[ll:ul:ndoc, idx] = np.sqrt(n[idx] * nw)
+        ck12[ll:ul:ndoc, ll:ul:ndoc] = -np.sqrt(np.outer(nw, nw))
+    return cj12, ck12
+
+
+def calcocce(gamma, J_MO, K_MO, H_core, p):
+    """The occupation energy E(gamma) (``pnof.py:994-1001``): softmax
+    occupations, GNOF coefficients, calce."""
+    n = ocupacion_softmax(gamma, p)
+    cj12, ck12 = cjckd8(n, p)
+    return calce(n, cj12, ck12, J_MO, K_MO, H_core, p)
+
+
 def orbital_gradient(elag, p):
     """Packed 4 (elag - elag^T) over i < nbf5, j > i (``pnof.py:1114-1131``)."""
     g = 4.0 * (elag - elag.T)

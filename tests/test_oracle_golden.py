@@ -163,3 +163,19 @@ def test_open_shell_fock_route():
     E, el1, sd, md = orc.energy1r(g["C"], g["n"], g["H"], None, g["b"], g["cj12"].copy(), g["ck12"].copy(), p)
     assert abs(E - float(g["E1r"])) < TOL * abs(E)
     assert nrel(el1, g["elag1r"]) < TOL
+
+
+@pytest.mark.parametrize("case", ["c1", "water", "ragged"])
+def test_occupations_coefficients_and_occupation_energy(case):
+    """The oracle's softmax occupations, CJCKD8 and calcocce against the
+    reference's own values (pnof.py:350-422, 770-809, 994-1001)."""
+    from oracle import pynof_oracle as orc
+
+    g = load_golden(case)
+    p = param_for(case)
+    n = orc.ocupacion_softmax(g["gamma"], p)
+    assert np.max(np.abs(n - g["n_soft"])) < 1e-15
+    cj, ck = orc.cjckd8(g["n_soft"], p)
+    assert np.max(np.abs(cj - g["cj12"])) < 1e-15 and np.max(np.abs(ck - g["ck12"])) < 1e-15
+    E = orc.calcocce(g["gamma"], g["J_MO_ri"], g["K_MO_ri"], g["H_core"], p)
+    assert abs(E - float(g["E_calcocce"])) < 1e-12 * abs(E)
