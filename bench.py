@@ -74,7 +74,7 @@ def parse():
     ap.add_argument("--maxit", type=int, default=200)
     ap.add_argument("--time-limit", type=float, default=None, help="seconds per served solve (serve mode)")
     ap.add_argument("--occ-nbf", default="60,300,600", help="nbf of the occupation problems (occ mode)")
-    ap.add_argument("--occupations", choices=["host", "device", "device_sync"], default="host",
+    ap.add_argument("--occupations", choices=["host", "device", "device_sync"], default="device_sync",
                     help="where served solves run the occupation CG (serve mode)")
     ap.add_argument("--serve-paths", default="mixed,fp64", help="precisions served in turn (serve mode)")
     return ap.parse_args()

@@ -949,7 +949,7 @@ int build_chunk_graph(OccState* st, int P, OccGraph& og) {
 // the phase copied back reads done (at most the evaluation cap's worth of
 // replays), then the occupations and C^J, C^K.  Synchronises `s` once per
 // replay.
-int run_host_driven(OccState* st, const OccArgs& a, OccGraph& og, cudaStream_t s, const char* name) {
+int run_host_driven(OccState* st, const OccArgs& a, const OccGraph& og, cudaStream_t s, const char* name) {
   occ_init_kernel<<<1, kStepThreads, 0, s>>>(st, a);
   GB_CHECK_LAUNCH(name);
   const long long maxev = 1 + 200LL * (a.maxiter + 1);
@@ -1015,7 +1015,7 @@ int occ_run(const double* gamma0, const double* J, const double* K, const double
   a.maxiter = maxiter;
   a.mode = mode;
   a.gtol = gtol;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::unique_lock<std::mutex> lk(g_mu);
   const auto key = std::make_tuple(gb::current_context_id(), (const void*)ws, nbf5);
   auto it = g_graphs.find(key);
   if (it == g_graphs.end()) {
@@ -1025,8 +1025,13 @@ int occ_run(const double* gamma0, const double* J, const double* K, const double
   }
   if (host_driven) {
     if (!it->second.chunk_exec) GB_TRY(build_chunk_graph(st, nbf5, it->second));
+    // the replay loop runs without the cache lock (other workspaces' calls
+    // proceed meanwhile); this workspace's entry stays until gb_occ_release,
+    // which must not overlap a call on the same workspace
+    const OccGraph og = it->second;
+    lk.unlock();
     const int pi = gb::prof_begin(name, s);
-    const int rc = run_host_driven(st, a, it->second, s, name);
+    const int rc = run_host_driven(st, a, og, s, name);
     gb::prof_end(pi, s);
     return rc;
   }

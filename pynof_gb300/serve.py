@@ -85,18 +85,20 @@ class Server:
     gradient falls.  precision "fp64": the plain DMMA path throughout.
     ``time_limit`` bounds each solve (seconds of its own wall time).
 
-    ``occupations`` chooses where each solve's occupation CG runs.  "host"
-    (the default here) is scipy's CG over the compiled evaluation, which
-    releases the GIL, on the host cores the saturated GPU leaves idle.  On a
-    config-5 stream (6 concurrent solves) it served 10.2 orbital steps/s
-    against 6.3 with the device graph ("device", :class:`ops.OccMinimizer`,
-    the default of a single solve), whose device-side loop slows the other
-    requests' GEMMs, and 6.0 driven from the host ("device_sync")."""
+    ``occupations`` chooses where each solve's occupation CG runs.
+    "device_sync" (the default here) runs the device kernels driven from the
+    host in replays of eight evaluations, which share the GPU evenly with
+    the other requests' GEMMs: on a config-5 stream (6 concurrent solves) it
+    served 14.0 orbital steps/s with 3 requests converged, against 10.2 and 2
+    for "host" (scipy's CG over the compiled evaluation on the host cores)
+    and 6.3 and 1 for "device" (the conditional-node graph, the default of a
+    single solve, whose device-side loop is served ahead of the other
+    requests' work)."""
 
     def __init__(self, hbm_budget: float = 150e9, slots: int = 8, precision: str = "mixed", nslices: int = 6,
                  fp64_switch: float | None = None, tol: float = 1e-5, maxit: int = 200, device=None,
                  ladder=None, final_fp64: bool = True, time_limit: float | None = None,
-                 occupations: str = "host"):
+                 occupations: str = "device_sync"):
         self.budget = int(hbm_budget)
         self.slots = slots
         self.precision = precision

@@ -14,10 +14,11 @@ def torch_cuda():
     return torch
 
 
-@pytest.mark.parametrize("occupations", ["host", "device"])
+@pytest.mark.parametrize("occupations", ["host", "device", "device_sync"])
 def test_alone_equals_in_mix(torch_cuda, occupations):
-    """With the occupation CG on the host or as each request's own device
-    graph (its own workspace, fixed-order reductions)."""
+    """With the occupation CG on the host, or on the device per request (its
+    own workspace and graphs, fixed-order reductions), from a conditional
+    node or driven from the host."""
     from pynof_gb300 import serve
 
     reqs = serve.poisson_stream(6, rate=200.0, nbf_lo=24, nbf_hi=48, seed=5)
