@@ -12,20 +12,22 @@
 //  - the pair sums over (a, b) from different pairs (calce, pnof.py:905-929,
 //    and the gradient of calcoccg, pnof.py:1004-1033 with der_CJCKD8,
 //    pnof.py:425-525): occ_rows_kernel, one warp per (32 orbitals a, 16
-//    orbitals b) item on a fixed grid, lanes over a so that J[b][a] and
-//    K[b][a] are read coalesced; per a: the energy terms, the dE/dn term and
-//    the two sums that give dE/dnd, each summed over the item's 16 pairs in
-//    a pairwise tree; the last warp to finish an a-group (an atomic count per
-//    group, no waiting) adds the group's items;
+//    orbitals b) item, lanes over a so that J[b][a] and K[b][a] are read
+//    coalesced.  The terms of a are linear in five weighted sums over b
+//    (n_b J_ba, n_b K_ba, and over the dynamic / static pairs fi_b K_ba,
+//    +-nd12_b K_ba, nd_b K_ba): at most five FMAs per pair.  The last warp to
+//    finish an a-group (an atomic count per group, no waiting) adds the
+//    group's items;
 //  - occ_step_kernel (one CTA): the diagonal and same-pair terms, the chain
 //    rule through nd = n F(n_s), g = dn^T e, and the energy -- the assembly
 //    of the host loop of occ_host.cu, summed in pairwise trees.
 //
 // GB300's FP64 unit has a long dependent latency (~64 clocks for an add or
 // FMA, several hundred for a division or square root, ~1000 for exp), so the
-// kernels are laid out for short FP64 dependency chains: every exponential
-// of a trial point in its own thread, the pair loop unrolled with masks,
-// tree sums, and the conjugate-gradient scalars of one evaluation from one
+// kernels are laid out for short FP64 dependency chains and few FP64
+// operations: every exponential of a trial point in its own thread, the pair
+// loop unrolled with masks into interleaved FMA chains, tree sums, and the
+// conjugate-gradient scalars of one evaluation from one
 // fused block reduction (the next search's g.g and g.p follow from it
 // algebraically).
 //
@@ -85,8 +87,8 @@ struct OccArgs {
   double *e, *en;                               // P
   double *ns, *F, *dF;                          // ndoc
   double *nw;                                   // nv
-  double *part;                                 // 4 P nbc (per item: energy, e, S1, S2)
-  double *row;                                  // 4 P (per orbital, all items)
+  double *part;                                 // 5 P nbc (per item: A1 .. A5)
+  double *row;                                  // 5 P (per orbital, all items)
   int *pair_of, *cls;                           // P
   unsigned int* grp;                            // per a-group: items done
   int P, no1, ndoc, ncwo, nv, nbc, maxiter, mode;
@@ -207,17 +209,12 @@ __device__ void prep_point(const OccArgs& a, const double* __restrict__ x) {
   __syncthreads();
 }
 
-// Pairwise sum of kBch values.
-__device__ __forceinline__ double tree16(double (&t)[kBch]) {
-#pragma unroll
-  for (int h = kBch / 2; h > 0; h >>= 1)
-#pragma unroll
-    for (int u = 0; u < h; ++u) t[u] += t[u + h];
-  return t[0];
-}
-
-// ---- pair sums over b for 32 orbitals a, then (last warp of the a-group)
-// the group's items added per orbital
+// ---- per orbital a, five weighted sums over the orbitals b of other pairs:
+// A1 = sum n_b J_ba, A2 = sum n_b K_ba and, over the pairs with the GNOF
+// dynamic / static terms (a strong and b weak, or a weak and b not core),
+// A3 = sum fi_b K_ba, A4 = sum s_ab nd12_b K_ba (s = -1 weak-weak),
+// A5 = sum nd_b K_ba.  The energy and gradient terms of a are linear in them
+// (assemble).  The last warp of an a-group adds the group's items.
 __global__ void __launch_bounds__(32) occ_rows_kernel(const OccState* __restrict__ st) {
   const OccArgs& a = st->a;
   if (st->phase == PH_DONE) return;
@@ -230,36 +227,31 @@ __global__ void __launch_bounds__(32) occ_rows_kernel(const OccState* __restrict
     const bool live = i < P;
     const int ii = live ? i : P - 1;
     const int pa = a.pair_of[ii], ca = a.cls[ii];
-    const double ni = a.n[ii], fii = a.fi[ii], fidi = a.fid[ii], nd12i = a.nd12[ii], ndi = a.nd[ii];
-    double tE[kBch], tea[kBch], tS1[kBch], tS2[kBch];
+    // two interleaved FMA chains per sum (even / odd b)
+    double s1[2] = {0.0, 0.0}, s2[2] = {0.0, 0.0}, s3[2] = {0.0, 0.0}, s4[2] = {0.0, 0.0}, s5[2] = {0.0, 0.0};
     const int b0 = bc * kBch;
 #pragma unroll
     for (int u = 0; u < kBch; ++u) {
       const int b = min(b0 + u, P - 1);
       const bool ok = b0 + u < P && b != ii && !(pa >= 0 && a.pair_of[b] == pa);
       const double Jba = a.J[(size_t)b * P + ii], Kba = a.K[(size_t)b * P + ii];
-      const double nb = a.n[b], fib = a.fi[b], nd12b = a.nd12[b], ndb = a.nd[b];
       const int cb = a.cls[b];
-      double ck = ni * nb, dck = nb, s1 = 0.0, s2 = 0.0;
-      if ((ca == 1 && cb == 2) || (ca == 2 && cb >= 1)) {
-        const double sg = (ca == 2 && cb == 2) ? -1.0 : 1.0;
-        ck += fii * fib + sg * nd12i * nd12b - ndi * ndb;
-        dck += fidi * fib;
-        s1 = sg * nd12b * Kba;
-        s2 = ndb * Kba;
-      }
-      tE[u] = ok ? 2.0 * ni * nb * Jba - ck * Kba : 0.0;
-      tea[u] = ok ? 4.0 * nb * Jba - 2.0 * dck * Kba : 0.0;
-      tS1[u] = ok ? s1 : 0.0;
-      tS2[u] = ok ? s2 : 0.0;
+      const double wn = ok ? a.n[b] : 0.0;
+      const bool chi = ok && ((ca == 1 && cb == 2) || (ca == 2 && cb >= 1));
+      const double sg = (ca == 2 && cb == 2) ? -1.0 : 1.0;
+      s1[u & 1] = fma(wn, Jba, s1[u & 1]);
+      s2[u & 1] = fma(wn, Kba, s2[u & 1]);
+      s3[u & 1] = fma(chi ? a.fi[b] : 0.0, Kba, s3[u & 1]);
+      s4[u & 1] = fma(chi ? sg * a.nd12[b] : 0.0, Kba, s4[u & 1]);
+      s5[u & 1] = fma(chi ? a.nd[b] : 0.0, Kba, s5[u & 1]);
     }
-    const double vE = tree16(tE), vea = tree16(tea), vS1 = tree16(tS1), vS2 = tree16(tS2);
     double* q = a.part + (size_t)ii * nbc + bc;
     if (live) {
-      q[0] = vE;
-      q[plane] = vea;
-      q[2 * plane] = vS1;
-      q[3 * plane] = vS2;
+      q[0] = s1[0] + s1[1];
+      q[plane] = s2[0] + s2[1];
+      q[2 * plane] = s3[0] + s3[1];
+      q[3 * plane] = s4[0] + s4[1];
+      q[4 * plane] = s5[0] + s5[1];
     }
     // the last of the group's nbc items adds them up (the counter is left at
     // zero for the next evaluation)
@@ -272,17 +264,12 @@ __global__ void __launch_bounds__(32) occ_rows_kernel(const OccState* __restrict
       __threadfence();
       if (live) {
         const double* r = a.part + (size_t)i * nbc;
-        double sE = 0.0, sea = 0.0, sS1 = 0.0, sS2 = 0.0;
-        for (int c = 0; c < nbc; ++c) {
-          sE += __ldcg(r + c);
-          sea += __ldcg(r + plane + c);
-          sS1 += __ldcg(r + 2 * plane + c);
-          sS2 += __ldcg(r + 3 * plane + c);
-        }
-        a.row[i] = sE;
-        a.row[P + i] = sea;
-        a.row[2 * P + i] = sS1;
-        a.row[3 * P + i] = sS2;
+        double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int c = 0; c < nbc; ++c)
+#pragma unroll
+          for (int k = 0; k < 5; ++k) t[k] += __ldcg(r + k * plane + c);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) a.row[k * P + i] = t[k];
       }
       if (lane == 0) a.grp[ag] = 0;
     }
@@ -295,9 +282,13 @@ __device__ double assemble(const OccArgs& a, double* sh) {
   double es = 0.0;
   for (int i = tid; i < P; i += kStepThreads) {
     const double d = 2.0 * a.H[i] + a.J[(size_t)i * P + i];
-    es += a.n[i] * d + a.row[i];
-    a.e[i] = d + a.row[P + i];
-    a.en[i] = -2.0 * (a.row[2 * P + i] / (2.0 * fmax(a.nd12[i], 1e-15)) - a.row[3 * P + i]);
+    const double A1 = a.row[i], A2 = a.row[P + i], A3 = a.row[2 * P + i], A4 = a.row[3 * P + i],
+                 A5 = a.row[4 * P + i];
+    const double ni = a.n[i];
+    // pairs (i, b), b of another pair: sum_b 2 n_i n_b J_bi - C^K_ib K_bi
+    es += ni * d + (2.0 * ni * A1 - ni * A2 - a.fi[i] * A3 - a.nd12[i] * A4 + a.nd[i] * A5);
+    a.e[i] = d + 4.0 * A1 - 2.0 * A2 - 2.0 * a.fid[i] * A3;
+    a.en[i] = -2.0 * (A4 / (2.0 * fmax(a.nd12[i], 1e-15)) - A5);
   }
   __syncthreads();
   // pairs inside one pair block: C^J = 0; C^K = sqrt(n_s n_w) (strong-weak),
@@ -795,8 +786,8 @@ void occ_layout(Cv& c, int P, int ndoc, int ncwo, OccState** state, OccArgs& a) 
   a.ns = c.template take<double>(ndoc);
   a.F = c.template take<double>(ndoc);
   a.dF = c.template take<double>(ndoc);
-  a.part = c.template take<double>((size_t)4 * P * nbc);
-  a.row = c.template take<double>((size_t)4 * P);
+  a.part = c.template take<double>((size_t)5 * P * nbc);
+  a.row = c.template take<double>((size_t)5 * P);
   a.pair_of = c.template take<int>(P);
   a.cls = c.template take<int>(P);
   a.grp = c.template take<unsigned int>((P + 31) / 32);
