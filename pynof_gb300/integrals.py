@@ -186,8 +186,8 @@ def metric_power(metric, alpha: float = -0.5, cutoff: float = 1.0e-14):
     dependency the reference does not pin): eigendecomposition of the
     symmetric metric; for a negative power, eigenvalues whose magnitude is
     below ``cutoff`` times the largest are dropped (their power is zero), the
-    others are raised to ``alpha``.  Host FP64 (LAPACK), as the north-star
-    keeps the metric inverse square root in FP64."""
+    others are raised to ``alpha``.  Host FP64 (LAPACK): the metric inverse
+    square root stays in FP64 on every precision form of the path."""
     a, V = np.linalg.eigh(np.asarray(metric, dtype=np.float64))
     amax = max(abs(a[0]), abs(a[-1])) if a.size else 0.0
     keep = ~((alpha < 0.0) & (np.abs(a) < cutoff * amax))
