@@ -5,8 +5,8 @@ The reference minimises the occupation energy over gamma with
 (``pynof/minimization.py:77-97``; ``p.occupation_optimizer = "CG"``,
 ``pynof/parameters.py:96``).  scipy is a dependency the reference does not pin
 (``pyproject.toml:15``); this module restates the published algorithm of its
-CG method as scipy 1.18 runs it, so that the device optimiser has a
-step-by-step checker:
+CG method as scipy 1.18 runs it, the step-by-step oracle of the device
+optimiser:
 
 * nonlinear conjugate gradients, Polak-Ribiere with the "+" restart
   (beta = max(0, g1.(g1 - g0) / g0.g0)), with the sufficient-descent check of

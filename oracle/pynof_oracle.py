@@ -1,7 +1,7 @@
 """CPU oracle for the RI / full-ERI JK and MO-integral path of PyNOF.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: the parity tests, the
-smoke check and the CPU-baseline leg of the benchmark import it.  Nothing in
+TEST INFRASTRUCTURE ONLY.  This module is the oracle of the parity tests, the
+smoke check and the CPU-baseline leg of the benchmark, which import it.  Nothing in
 the ``pynof_gb300`` package imports it, and no product code path runs through
 it.
 
