@@ -294,7 +294,8 @@ int gb_occ_minimize_dev_sync(const double* gamma0, const double* J_MO, const dou
 int gb_occ_energy_grad_dev(const double* gamma, const double* J_MO, const double* K_MO, const double* H_core,
                            int nbf5, int no1, int ndoc, int ncwo, double* result, double* grad, void* ws,
                            size_t ws_bytes, void* stream);
-/* Drop the cached graph of a workspace (before freeing it). */
+/* Drop the cached graphs of a workspace (before freeing it; a graph still in
+ * flight is freed when it completes).  No call on the workspace may overlap. */
 int gb_occ_release(const void* ws);
 
 /* Plain FP64 GEMM C = A B^T with row-major A [M][K], B [N][K], C [M][N] on the

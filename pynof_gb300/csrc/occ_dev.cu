@@ -799,11 +799,9 @@ struct OccGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraphNode_t init = nullptr;
-  // host-driven form: kChunk evaluations as an ordinary graph, and a pinned
-  // word the phase is copied into after each replay
+  // host-driven form: kChunk evaluations as an ordinary graph
   cudaGraph_t chunk_graph = nullptr;
   cudaGraphExec_t chunk_exec = nullptr;
-  int* flag = nullptr;
 };
 
 constexpr int kChunk = 8;  // evaluations per replay of the host-driven form
@@ -924,22 +922,16 @@ int build_chunk_graph(OccState* st, int P, OccGraph& og) {
   cudaGraphExec_t exec = nullptr;
   cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
   if (e != cudaSuccess) return fail(e, "occ chunk graph: instantiate");
-  int* flag = nullptr;
-  e = cudaHostAlloc(&flag, sizeof(int), cudaHostAllocDefault);
-  if (e != cudaSuccess) {
-    cudaGraphExecDestroy(exec);
-    return fail(e, "occ chunk graph: pinned flag");
-  }
   og.chunk_graph = g;
   og.chunk_exec = exec;
-  og.flag = flag;
   return GB_OK;
 }
 
 // The host-driven minimisation: init, then replays of the chunk graph until
 // the phase copied back reads done (at most the evaluation cap's worth of
-// replays), then the occupations and C^J, C^K.  Synchronises `s` once per
-// replay.
+// replays), then the occupations and C^J, C^K.  The phase comes back through
+// a stream-ordered copy to pageable memory (it returns once the replay has
+// run), so nothing synchronises more than `s`.
 int run_host_driven(OccState* st, const OccArgs& a, const OccGraph& og, cudaStream_t s, const char* name) {
   occ_init_kernel<<<1, kStepThreads, 0, s>>>(st, a);
   GB_CHECK_LAUNCH(name);
@@ -948,11 +940,10 @@ int run_host_driven(OccState* st, const OccArgs& a, const OccGraph& og, cudaStre
   int phase = PH_INIT;
   for (long long r = 0; r < max_replays && phase != PH_DONE; ++r) {
     GB_TRY(gb::cuda_status(cudaGraphLaunch(og.chunk_exec, s), name));
-    GB_TRY(gb::cuda_status(cudaMemcpyAsync(og.flag, reinterpret_cast<const char*>(st) + offsetof(OccState, phase),
+    GB_TRY(gb::cuda_status(cudaMemcpyAsync(&phase, reinterpret_cast<const char*>(st) + offsetof(OccState, phase),
                                            sizeof(int), cudaMemcpyDeviceToHost, s),
                            name));
     GB_TRY(gb::cuda_status(cudaStreamSynchronize(s), name));
-    phase = *og.flag;
   }
   GB_REQUIRE(phase == PH_DONE, GB_ERR_TIMEOUT, "%s: the minimiser did not stop within the evaluation cap", name);
   occ_final_kernel<<<1, kStepThreads, 0, s>>>(st);
@@ -1082,7 +1073,6 @@ extern "C" int gb_occ_release(const void* ws) {
       cudaGraphDestroy(it->second.graph);
       if (it->second.chunk_exec) cudaGraphExecDestroy(it->second.chunk_exec);
       if (it->second.chunk_graph) cudaGraphDestroy(it->second.chunk_graph);
-      if (it->second.flag) cudaFreeHost(it->second.flag);
       it = g_graphs.erase(it);
     } else {
       ++it;

@@ -421,18 +421,18 @@ class OccMinimizer:
         return self.result, self.grad
 
     def close(self) -> None:
-        """Drop the library's cached graph for this workspace (after the
-        stream's work on it has finished)."""
+        """Drop the library's cached graphs for this workspace.  A graph still
+        running is freed when it completes (cudaGraphExecDestroy), and the
+        workspace memory returns to torch's allocator in stream order, so no
+        synchronisation is needed -- in a server, a device-wide one would wait
+        for every other request's work."""
         if self._ws is not None:
-            torch.cuda.current_stream(self.device).synchronize()
             _lib.call("gb_occ_release", self._wp)
             self._ws = None
 
     def __del__(self):
         try:
-            if self._ws is not None and torch.cuda.is_available():
-                torch.cuda.synchronize(self.device)
-                _lib.call("gb_occ_release", self._wp)
+            self.close()
         except Exception:
             pass
 
